@@ -1,0 +1,126 @@
+/*
+ * qcu_gb300.h -- extensions of the drop-in ABI in qcu.h.
+ *
+ * None of these has a counterpart in the reference unless a line says so;
+ * they expose what the reference's C ABI hides or lacks: an error status, the
+ * boundary condition, explicit streams, device-resident MRHS fields (no
+ * per-call layout transform), the layout transforms themselves, the Krylov
+ * solvers and the kernel autotuner.
+ *
+ * Every function returns 0 (QCU_OK) or one of the QCU_ERR_* codes below and
+ * records the error for qcuGetLastError().  Pointers are device pointers.
+ *
+ * Internal MRHS field of one parity (for the session lattice and N):
+ *   data  [Vh][4N][nrhs] complex in the field precision (RHS innermost)
+ *   norm  [Vh][nrhs] float, present only for 16-bit storage; stored values
+ *         are component / norm(site, rhs)
+ * Sizes come from qcuFieldBytes.  Buffers must be 16-byte aligned.
+ */
+#pragma once
+
+#include <stddef.h>
+
+#include "qcu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+typedef enum QcuStatus_e {
+  QCU_OK = 0,
+  QCU_ERR_NOT_INITIALIZED = 1,
+  QCU_ERR_INVALID_ARGUMENT = 2,
+  QCU_ERR_UNSUPPORTED = 3,
+  QCU_ERR_CUDA = 4,
+  QCU_ERR_NO_GAUGE = 5,
+  QCU_ERR_NO_OPERATOR = 6,
+  QCU_ERR_NOT_CONVERGED = 7,
+  QCU_ERR_BREAKDOWN = 8,
+  QCU_ERR_DEVICE_TIMEOUT = 9,
+  QCU_ERR_OUT_OF_MEMORY = 10,
+  QCU_ERR_CAPACITY = 11
+} QcuStatus;
+
+/* precision codes: the reference's QCU_PRECISION values
+ * (include/qcu_enum.h:4 of the reference) plus BF16 */
+#define QCU_HALF_PRECISION 0
+#define QCU_SINGLE_PRECISION 1
+#define QCU_DOUBLE_PRECISION 2
+#define QCU_BF16_PRECISION 4
+
+/* caller fermion address modes for pack/unpack */
+#define QCU_SRC_EO_HALF 0 /* one parity [Vh][4][N] */
+#define QCU_SRC_EO_FULL 1 /* [2][Vh][4][N]; parity selects the half */
+#define QCU_SRC_LEX 2     /* lexicographic full field [V][4][N] */
+
+/* solvers */
+#define QCU_SOLVER_CG 0       /* CG on Mhat^dag Mhat, Mhat = 1 - kappa^2 D_eo D_oe */
+#define QCU_SOLVER_BICGSTAB 1 /* BiCGStab on Mhat */
+
+int qcuGetLastError(void);
+const char *qcuGetLastErrorString(void);
+void qcuClearError(void);
+const char *qcuVersion(void);
+
+/* 1 = antiperiodic time boundaries (every hop across t = Lt-1 <-> 0 is
+ * multiplied by -1), 0 = periodic (the reference's only mode). */
+int qcuSetAntiperiodicT(int flag);
+/* Run library work on this cudaStream_t (NULL: the library's own stream).
+ * ABI calls still synchronise before returning. */
+int qcuSetStream(void *stream);
+int qcuSynchronize(void);
+
+/* bytes of one internal MRHS field of one parity */
+int qcuFieldBytes(int precision, int nrhs, size_t *data_bytes, size_t *norm_bytes);
+
+/* caller FP64 fermions -> internal MRHS field (one launch for all RHS) */
+int qcuPackFermions(void *dst, void *dst_norm, void *const *src, int nrhs, int src_mode, int parity, int precision);
+/* internal MRHS field -> caller FP64 fermions */
+int qcuUnpackFermions(void *const *dst, const void *src, const void *src_norm, int nrhs, int dst_mode, int parity,
+                      int precision);
+
+/* load a lexicographic gauge field [4][V][N][N] (complex double) */
+int qcuLoadGaugeLex(void *gauge_lex);
+/* lexicographic [V][ncomp] <-> even-odd [2][Vh][ncomp] complex double */
+int qcuLexToEo(void *eo_out, const void *lex_in, int ncomp);
+int qcuEoToLex(void *lex_out, const void *eo_in, int ncomp);
+
+/* out = D_parity^f in on resident MRHS fields; precision as in getDslash
+ * (the session gauge is converted to it once).  Asynchronous on the
+ * library stream. */
+int qcuDslashMRHS(void *out, void *out_norm, const void *in, const void *in_norm, int nrhs, int parity, int dagger,
+                  int precision);
+/* out = a * D_parity^f in + b * x  (the reference's DslashXpay stub,
+ * include/qcu_dirac.h:49) */
+int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_norm, const void *x,
+                      const void *x_norm, int nrhs, int parity, int dagger, int precision, double a, double b);
+
+/* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
+ * Returns the chosen RHS-per-thread and block size. */
+int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block);
+
+typedef struct QcuSolverParam_s {
+  int solver;          /* QCU_SOLVER_CG or QCU_SOLVER_BICGSTAB */
+  int inner_precision; /* operator precision of the inner iterations */
+  double kappa;
+  double tol;          /* target |b - M x| / |b| per RHS (FP64 true residual) */
+  int max_iter;
+  double delta;        /* reliable-update trigger: |r| < delta * max|r| since the last update */
+  int use_graph;       /* capture inner iterations in CUDA graphs */
+  int src_mode;        /* QCU_SRC_EO_FULL or QCU_SRC_LEX for x and b */
+  /* outputs */
+  int iterations;
+  int reliable_updates;
+  double seconds;
+  double true_residual[256]; /* per RHS, FP64 */
+  int converged[256];
+} QcuSolverParam;
+
+void qcuSolverParamDefaults(QcuSolverParam *p);
+/* Solve M x_r = b_r for nrhs right-hand sides with the loaded gauge. */
+int qcuInvert(void *const *x, void *const *b, int nrhs, QcuSolverParam *p);
+
+#ifdef __cplusplus
+}
+#endif

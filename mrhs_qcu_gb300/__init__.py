@@ -1,0 +1,297 @@
+"""mrhs_qcu_gb300 -- GB300 (sm_103a) multi-right-hand-side even-odd Wilson
+dslash, layout transforms and even-odd preconditioned Krylov solves behind
+the reference's ``qcu.h`` C ABI.
+
+The compute path is ``libqcu.so`` (CUDA kernels + C++ host layer, built
+in-tree by ``mrhs_qcu_gb300.build``).  This module is a thin ctypes mirror of
+the C ABI with the reference's function names (include/qcu.h:19-30 of the
+reference) plus the extensions of ``include/qcu_gb300.h``.  There is no CPU
+fallback: importing fails if the library has not been built.
+
+Pointers are device addresses (ints), e.g. ``tensor.data_ptr()`` of a CUDA
+tensor of dtype complex128 in the caller layouts documented in qcu.h.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libqcu.so")
+
+# enum values of the reference (include/qcu_enum.h:4-12) + BF16 extension
+QCU_HALF_PRECISION = 0
+QCU_SINGLE_PRECISION = 1
+QCU_DOUBLE_PRECISION = 2
+QCU_BF16_PRECISION = 4
+EVEN_PARITY = 0
+ODD_PARITY = 1
+QCU_DAGGER_NO = 0
+QCU_DAGGER_YES = 1
+DSLASH_WILSON = 0
+DSLASH_CLOVER = 1
+
+QCU_SRC_EO_HALF = 0
+QCU_SRC_EO_FULL = 1
+QCU_SRC_LEX = 2
+QCU_SOLVER_CG = 0
+QCU_SOLVER_BICGSTAB = 1
+
+STATUS = {0: "QCU_OK", 1: "QCU_ERR_NOT_INITIALIZED", 2: "QCU_ERR_INVALID_ARGUMENT", 3: "QCU_ERR_UNSUPPORTED",
+          4: "QCU_ERR_CUDA", 5: "QCU_ERR_NO_GAUGE", 6: "QCU_ERR_NO_OPERATOR", 7: "QCU_ERR_NOT_CONVERGED",
+          8: "QCU_ERR_BREAKDOWN", 9: "QCU_ERR_DEVICE_TIMEOUT", 10: "QCU_ERR_OUT_OF_MEMORY",
+          11: "QCU_ERR_CAPACITY"}
+
+
+class QcuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(code, code), msg.strip()))
+        self.code = code
+
+
+class QcuParam(ctypes.Structure):
+    """include/qcu.h:7-9 of the reference."""
+    _fields_ = [("lattice_size", ctypes.c_int * 4)]
+
+
+class QcuGrid(ctypes.Structure):
+    """include/qcu.h:11-15 of the reference."""
+    _fields_ = [("grid_size", ctypes.c_int * 4)]
+
+
+class QcuSolverParam(ctypes.Structure):
+    _fields_ = [("solver", ctypes.c_int), ("inner_precision", ctypes.c_int), ("kappa", ctypes.c_double),
+                ("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("delta", ctypes.c_double),
+                ("use_graph", ctypes.c_int), ("src_mode", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("reliable_updates", ctypes.c_int), ("seconds", ctypes.c_double),
+                ("true_residual", ctypes.c_double * 256), ("converged", ctypes.c_int * 256)]
+
+
+# every symbol the public headers declare (include/qcu.h, include/qcu_gb300.h)
+ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge", "getDslash", "dslashQcu",
+               "fullDslashQcu", "cg_inverter"]
+EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
+               "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
+               "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
+               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert"]
+# C++ symbols with the reference's mangled names (include/qcu_storage.h)
+CXX_SYMBOLS = ["_ZN3qcu7storage18shiftVectorStorageEPvS1_14ShiftDirectioniiii",
+               "_ZN3qcu7storage17shiftGaugeStorageEPvS1_14ShiftDirectioniiii"]
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libqcu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libqcu.so is not built: run `python -m mrhs_qcu_gb300.build` "
+                          "(or __graft_entry__.build()); there is no CPU fallback")
+    L = ctypes.CDLL(LIB_PATH)
+    P, I, D, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_size_t
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "initGridSize": ([ctypes.POINTER(QcuGrid), ctypes.POINTER(QcuParam), I], None),
+        "pushBackFermions": ([P, P], None),
+        "startDslash": ([I, I], None),
+        "loadQcuGauge": ([P], None),
+        "getDslash": ([I, D, I, I, I], None),
+        "dslashQcu": ([P, P, P, ctypes.POINTER(QcuParam), I], None),
+        "fullDslashQcu": ([P, P, P, ctypes.POINTER(QcuParam), I], None),
+        "cg_inverter": ([P, P, P, ctypes.POINTER(QcuParam), D, D], None),
+        "qcuGetLastError": ([], I),
+        "qcuGetLastErrorString": ([], ctypes.c_char_p),
+        "qcuClearError": ([], None),
+        "qcuVersion": ([], ctypes.c_char_p),
+        "qcuSetAntiperiodicT": ([I], I),
+        "qcuSetStream": ([P], I),
+        "qcuSynchronize": ([], I),
+        "qcuFieldBytes": ([I, I, ctypes.POINTER(S), ctypes.POINTER(S)], I),
+        "qcuPackFermions": ([P, P, PP, I, I, I, I], I),
+        "qcuUnpackFermions": ([PP, P, P, I, I, I, I], I),
+        "qcuLoadGaugeLex": ([P], I),
+        "qcuLexToEo": ([P, P, I], I),
+        "qcuEoToLex": ([P, P, I], I),
+        "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
+        "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
+        "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
+        "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _p(x):
+    return ctypes.c_void_p(int(x)) if x is not None else None
+
+
+def _ptrs(xs):
+    arr = (ctypes.c_void_p * len(xs))(*[int(x) for x in xs])
+    return ctypes.cast(arr, ctypes.POINTER(ctypes.c_void_p)), arr
+
+
+def last_error():
+    L = lib()
+    return L.qcuGetLastError(), (L.qcuGetLastErrorString() or b"").decode()
+
+
+def clear_error():
+    lib().qcuClearError()
+
+
+def _raise_if(code=None):
+    L = lib()
+    c = L.qcuGetLastError() if code is None else code
+    if c != 0:
+        msg = (L.qcuGetLastErrorString() or b"").decode()
+        L.qcuClearError()
+        raise QcuError(c, msg)
+
+
+def _param(L4):
+    p = QcuParam()
+    for i in range(4):
+        p.lattice_size[i] = int(L4[i])
+    return p
+
+
+# ---- the reference's C ABI (void functions; errors raise QcuError) ----------
+def initGridSize(lattice, nColors: int = 3, grid=(1, 1, 1, 1)) -> None:
+    clear_error()
+    g = QcuGrid()
+    for i in range(4):
+        g.grid_size[i] = int(grid[i])
+    p = _param(lattice)
+    lib().initGridSize(ctypes.byref(g), ctypes.byref(p), int(nColors))
+    _raise_if()
+
+
+def loadQcuGauge(gauge_ptr) -> None:
+    clear_error()
+    lib().loadQcuGauge(_p(gauge_ptr))
+    _raise_if()
+
+
+def getDslash(dslashType: int, mass: float, nColors: int, nInputs: int, floatPrecision: int) -> None:
+    clear_error()
+    lib().getDslash(int(dslashType), float(mass), int(nColors), int(nInputs), int(floatPrecision))
+    _raise_if()
+
+
+def pushBackFermions(fermionOut_ptr, fermionIn_ptr) -> None:
+    clear_error()
+    lib().pushBackFermions(_p(fermionOut_ptr), _p(fermionIn_ptr))
+    _raise_if()
+
+
+def startDslash(parity: int, daggerFlag: int = 0) -> None:
+    clear_error()
+    lib().startDslash(int(parity), int(daggerFlag))
+    _raise_if()
+
+
+def dslashQcu(out_ptr, in_ptr, gauge_ptr, lattice, parity: int) -> None:
+    clear_error()
+    p = _param(lattice)
+    lib().dslashQcu(_p(out_ptr), _p(in_ptr), _p(gauge_ptr), ctypes.byref(p), int(parity))
+    _raise_if()
+
+
+def fullDslashQcu(out_ptr, in_ptr, gauge_ptr, lattice, dagger_flag: int) -> None:
+    clear_error()
+    p = _param(lattice)
+    lib().fullDslashQcu(_p(out_ptr), _p(in_ptr), _p(gauge_ptr), ctypes.byref(p), int(dagger_flag))
+    _raise_if()
+
+
+def cg_inverter(x_ptr, b_ptr, gauge_ptr, lattice, p_max_prec: float, p_kappa: float) -> None:
+    clear_error()
+    p = _param(lattice)
+    lib().cg_inverter(_p(x_ptr), _p(b_ptr), _p(gauge_ptr), ctypes.byref(p), float(p_max_prec), float(p_kappa))
+    _raise_if()
+
+
+# ---- extensions ----------------------------------------------------------
+def set_antiperiodic_t(flag: bool) -> None:
+    _raise_if(lib().qcuSetAntiperiodicT(int(bool(flag))))
+
+
+def set_stream(stream_handle) -> None:
+    _raise_if(lib().qcuSetStream(_p(stream_handle) if stream_handle else None))
+
+
+def synchronize() -> None:
+    _raise_if(lib().qcuSynchronize())
+
+
+def field_bytes(precision: int, nrhs: int):
+    d, n = ctypes.c_size_t(), ctypes.c_size_t()
+    _raise_if(lib().qcuFieldBytes(int(precision), int(nrhs), ctypes.byref(d), ctypes.byref(n)))
+    return d.value, n.value
+
+
+def pack_fermions(dst, dst_norm, srcs, src_mode: int, parity: int, precision: int) -> None:
+    pp, keep = _ptrs(srcs)
+    _raise_if(lib().qcuPackFermions(_p(dst), _p(dst_norm), pp, len(srcs), int(src_mode), int(parity),
+                                    int(precision)))
+
+
+def unpack_fermions(dsts, src, src_norm, dst_mode: int, parity: int, precision: int) -> None:
+    pp, keep = _ptrs(dsts)
+    _raise_if(lib().qcuUnpackFermions(pp, _p(src), _p(src_norm), len(dsts), int(dst_mode), int(parity),
+                                      int(precision)))
+
+
+def load_gauge_lex(ptr) -> None:
+    _raise_if(lib().qcuLoadGaugeLex(_p(ptr)))
+
+
+def lex_to_eo(eo_out, lex_in, ncomp: int) -> None:
+    _raise_if(lib().qcuLexToEo(_p(eo_out), _p(lex_in), int(ncomp)))
+
+
+def eo_to_lex(lex_out, eo_in, ncomp: int) -> None:
+    _raise_if(lib().qcuEoToLex(_p(lex_out), _p(eo_in), int(ncomp)))
+
+
+def dslash_mrhs(out, out_norm, inp, in_norm, nrhs: int, parity: int, dagger: int, precision: int) -> None:
+    _raise_if(lib().qcuDslashMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), int(nrhs), int(parity), int(dagger),
+                                  int(precision)))
+
+
+def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: int, dagger: int, precision: int,
+                     a: float, b: float) -> None:
+    _raise_if(lib().qcuDslashXpayMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), _p(x), _p(x_norm), int(nrhs),
+                                      int(parity), int(dagger), int(precision), float(a), float(b)))
+
+
+def tune_dslash(nrhs: int, precision: int):
+    R, B = ctypes.c_int(), ctypes.c_int()
+    _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B)))
+    return R.value, B.value
+
+
+def solver_params(**kw) -> QcuSolverParam:
+    p = QcuSolverParam()
+    lib().qcuSolverParamDefaults(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def invert(xs, bs, params: QcuSolverParam, raise_on_error: bool = True) -> QcuSolverParam:
+    px, kx = _ptrs(xs)
+    pb, kb = _ptrs(bs)
+    rc = lib().qcuInvert(px, pb, len(xs), ctypes.byref(params))
+    if raise_on_error:
+        _raise_if(rc)
+    else:
+        clear_error()
+    return params

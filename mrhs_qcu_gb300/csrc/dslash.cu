@@ -1,0 +1,52 @@
+// Dslash registry and launch (see dslash.h).
+#include <map>
+#include <mutex>
+
+#include "dslash.h"
+
+namespace qcu {
+namespace {
+std::map<int, DslashLauncher>& registry() {
+  static std::map<int, DslashLauncher> r;
+  return r;
+}
+std::mutex& registry_mutex() {
+  static std::mutex m;
+  return m;
+}
+int key(int prec, int N, int R) { return (prec * 16 + N) * 16 + R; }
+}  // namespace
+
+void register_dslash(int prec, int N, int R, DslashLauncher fn) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  registry()[key(prec, N, R)] = fn;
+}
+
+DslashLauncher find_dslash(int prec, int N, int R) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  auto it = registry().find(key(prec, N, R));
+  return it == registry().end() ? nullptr : it->second;
+}
+
+int dslash_r_options(int prec, int N, int* out, int max) {
+  int n = 0;
+  for (int R = 8; R >= 1 && n < max; R--)
+    if (find_dslash(prec, N, R)) out[n++] = R;
+  return n;
+}
+
+void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st) {
+  DslashLauncher fn = find_dslash(prec, N, cfg.R);
+  QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
+              std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +
+                  ", R=" + std::to_string(cfg.R));
+  QCU_REQUIRE(A.nrhs % cfg.R == 0, QCU_ERR_INVALID_ARGUMENT, "nrhs not a multiple of R");
+  QCU_REQUIRE((int64_t)A.geo.vh * (A.nrhs / cfg.R) < (1ll << 31), QCU_ERR_INVALID_ARGUMENT,
+              "lattice x nrhs too large for one launch");
+  DslashArgs B = A;
+  B.div_groups = FastDiv((uint32_t)(A.nrhs / cfg.R));
+  fn(B, cfg.block, st);
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace qcu

@@ -1,0 +1,30 @@
+// Dslash dispatch: runtime (precision, N, RHS per thread) -> kernel instance.
+// This is the GB300 counterpart of the reference's instantiateDslash ladder
+// (src/qcd/qcu_wilson.cu:61-173): every (precision, N) pair has its own
+// instances, N = 6, 7, 8 included (the reference maps them to N = 5,
+// src/qcd/qcu_wilson.cu:109-119), and nrhs is a runtime value split into
+// groups of R RHS per thread instead of a compile-time 1..5.
+#pragma once
+
+#include "dslash_kernel.cuh"
+
+namespace qcu {
+
+using DslashLauncher = void (*)(const DslashArgs&, int block, cudaStream_t);
+
+// registry filled by the instantiation units (dslash_inst_*.cu)
+DslashLauncher find_dslash(int prec, int N, int R);
+void register_dslash(int prec, int N, int R, DslashLauncher fn);
+
+// RHS-per-thread values compiled for (prec, N), largest first
+int dslash_r_options(int prec, int N, int* out, int max);
+
+struct DslashConfig {
+  int R = 1;
+  int block = 128;
+};
+
+// launch with an explicit configuration (throws if not compiled)
+void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st);
+
+}  // namespace qcu

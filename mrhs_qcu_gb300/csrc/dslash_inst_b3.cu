@@ -1,0 +1,15 @@
+// Dslash instances for PREC_BF16; registered at library load.
+#include "dslash.h"
+
+namespace qcu {
+namespace {
+struct Register_b3 {
+  Register_b3() {
+    register_dslash(PREC_BF16, 3, 1, &launch_wilson_mrhs<PREC_BF16, 3, 1>);
+    register_dslash(PREC_BF16, 3, 2, &launch_wilson_mrhs<PREC_BF16, 3, 2>);
+    register_dslash(PREC_BF16, 3, 3, &launch_wilson_mrhs<PREC_BF16, 3, 3>);
+    register_dslash(PREC_BF16, 3, 4, &launch_wilson_mrhs<PREC_BF16, 3, 4>);
+  }
+} register_b3;
+}  // namespace
+}  // namespace qcu

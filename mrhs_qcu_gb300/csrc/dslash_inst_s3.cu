@@ -1,0 +1,15 @@
+// Dslash instances for PREC_SINGLE; registered at library load.
+#include "dslash.h"
+
+namespace qcu {
+namespace {
+struct Register_s3 {
+  Register_s3() {
+    register_dslash(PREC_SINGLE, 3, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 1>);
+    register_dslash(PREC_SINGLE, 3, 2, &launch_wilson_mrhs<PREC_SINGLE, 3, 2>);
+    register_dslash(PREC_SINGLE, 3, 3, &launch_wilson_mrhs<PREC_SINGLE, 3, 3>);
+    register_dslash(PREC_SINGLE, 3, 4, &launch_wilson_mrhs<PREC_SINGLE, 3, 4>);
+  }
+} register_s3;
+}  // namespace
+}  // namespace qcu

@@ -1,0 +1,347 @@
+// Layout transforms between the caller formats of qcu.h and the internal
+// device layouts.
+//
+// Caller formats (complex double, the reference's "non-coalesced" layouts,
+// include/kernels/storage/storage_kernels.cuh:14-101 of the reference):
+//   fermion, one parity      [Vh][4][N]
+//   fermion, full, eo split  [2][Vh][4][N]   (even half first)
+//   fermion, lexicographic   [V][4][N]       (site ((t*Lz+z)*Ly+y)*Lx+X)
+//   gauge, eo split          [4][2][Vh][N][N]
+//   gauge, lexicographic     [4][V][N][N]
+// Internal formats: see qcu_common.cuh.
+//
+// The reference converts one RHS per launch, double SU(3) only
+// (src/storage/qcu_storage.cu:9-35).  Here one launch packs every queued RHS
+// into one RHS-innermost MRHS field in the target precision (computing the
+// per-(site, RHS) scale for 16-bit storage), and the source may be
+// lexicographic: the lexicographic -> even-odd map is applied on the fly.
+#include <algorithm>
+
+#include "layout.h"
+
+namespace qcu {
+namespace {
+
+// half-site i of parity p -> source site offset (in units of 4N complexes)
+__device__ __forceinline__ int64_t src_site(int mode, int64_t i, int p, const Geometry& g) {
+  if (mode == SRC_EO_HALF) return i;
+  if (mode == SRC_EO_FULL) return (int64_t)p * g.vh + i;
+  // lexicographic
+  uint32_t rest, xh, y, z, t, rest2;
+  g.div_hx.divmod((uint32_t)i, rest, xh);
+  g.div_y.divmod(rest, rest2, y);
+  g.div_z.divmod(rest2, t, z);
+  const int X = 2 * (int)xh + (p ^ (int)((y + z + t) & 1));
+  return (((int64_t)t * g.L[2] + z) * g.L[1] + y) * g.L[0] + X;
+}
+
+template <int P, int N>
+__global__ void pack_fermions_kernel(PtrArray src, int mode, int parity, void* dst, float* dst_norm, Geometry g,
+                                     int nrhs, FastDiv div_nrhs) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t site, r;
+  div_nrhs.divmod(gid, site, r);
+  if ((int)site >= g.vh) return;
+  const double2* s = static_cast<const double2*>(src.p[r]) + src_site(mode, site, parity, g) * (4 * N);
+  double2 v[4 * N];
+#pragma unroll
+  for (int c = 0; c < 4 * N; c++) v[c] = __ldg(s + c);
+  E* d = static_cast<E*>(dst) + (int64_t)site * 4 * N * nrhs + r;
+  if constexpr (S::has_norm) {
+    double m = 0.0;
+#pragma unroll
+    for (int c = 0; c < 4 * N; c++) m = fmax(m, fmax(fabs(v[c].x), fabs(v[c].y)));
+    const float mf = (float)m;
+    const double inv = m > 0.0 ? 1.0 / (double)mf : 0.0;
+    dst_norm[(int64_t)site * nrhs + r] = mf;
+#pragma unroll
+    for (int c = 0; c < 4 * N; c++) d[(int64_t)c * nrhs] = S::from_c(make_float2((float)(v[c].x * inv), (float)(v[c].y * inv)));
+  } else {
+#pragma unroll
+    for (int c = 0; c < 4 * N; c++) {
+      E e;
+      e.x = v[c].x;
+      e.y = v[c].y;
+      d[(int64_t)c * nrhs] = e;
+    }
+  }
+}
+
+template <int P, int N>
+__global__ void unpack_fermions_kernel(PtrArray dstp, int mode, int parity, const void* src, const float* src_norm,
+                                       Geometry g, int nrhs, FastDiv div_nrhs) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t site, r;
+  div_nrhs.divmod(gid, site, r);
+  if ((int)site >= g.vh) return;
+  const E* s = static_cast<const E*>(src) + (int64_t)site * 4 * N * nrhs + r;
+  double2* d = static_cast<double2*>(const_cast<void*>(dstp.p[r])) + src_site(mode, site, parity, g) * (4 * N);
+  double scale = 1.0;
+  if constexpr (S::has_norm) scale = (double)src_norm[(int64_t)site * nrhs + r];
+#pragma unroll
+  for (int c = 0; c < 4 * N; c++) {
+    auto v = S::to_c(s[(int64_t)c * nrhs]);
+    d[c] = make_double2((double)v.x * scale, (double)v.y * scale);
+  }
+}
+
+// gauge: caller (eo or lexicographic) complex double -> [4][2][N*N][Vh] P
+template <int P>
+__global__ void pack_gauge_kernel(const double2* __restrict__ src, int lex, void* dst, Geometry g, int nn) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // over 4 * 2 * vh
+  if (gid >= (int64_t)8 * g.vh) return;
+  const int64_t i = gid % g.vh;
+  const int mp = (int)(gid / g.vh);  // mu * 2 + parity
+  const int mu = mp >> 1, p = mp & 1;
+  int64_t s;
+  if (lex)
+    s = (int64_t)mu * 2 * g.vh + src_site(SRC_LEX, i, p, g);
+  else
+    s = (int64_t)mp * g.vh + i;
+  const double2* a = src + s * nn;
+  E* d = static_cast<E*>(dst) + (int64_t)mp * nn * g.vh + i;
+  for (int k = 0; k < nn; k++) {
+    double2 v = __ldg(a + k);
+    E e;
+    if constexpr (P == PREC_DOUBLE) {
+      e = v;
+    } else if constexpr (P == PREC_SINGLE) {
+      e = make_float2((float)v.x, (float)v.y);
+    } else {
+      e = S::from_c(make_float2((float)v.x, (float)v.y));
+    }
+    d[(int64_t)k * g.vh] = e;
+  }
+}
+
+// internal FP64 gauge -> caller eo layout (the reference's TO_NON_COALESCE)
+__global__ void unpack_gauge_kernel(const double2* __restrict__ src, double2* dst, int vh, int nn) {
+  const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (int64_t)8 * vh) return;
+  const int64_t i = gid % vh;
+  const int mp = (int)(gid / vh);
+  const double2* s = src + (int64_t)mp * nn * vh + i;
+  double2* d = dst + ((int64_t)mp * vh + i) * nn;
+  for (int k = 0; k < nn; k++) d[k] = s[(int64_t)k * vh];
+}
+
+// convert an MRHS field between storage precisions (same layout)
+template <int PI, int PO>
+__global__ void convert_field_kernel(const void* src, const float* src_norm, void* dst, float* dst_norm,
+                                     int64_t vh, int ncomp, int nrhs, FastDiv div_nrhs) {
+  using SI = Store<PI>;
+  using SO = Store<PO>;
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t site, r;
+  div_nrhs.divmod(gid, site, r);
+  if ((int64_t)site >= vh) return;
+  const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * ncomp * nrhs + r;
+  auto* d = static_cast<typename SO::elem*>(dst) + (int64_t)site * ncomp * nrhs + r;
+  double si = 1.0;
+  if constexpr (SI::has_norm) si = (double)src_norm[(int64_t)site * nrhs + r];
+  double m = 0.0;
+  if constexpr (SO::has_norm) {
+    for (int c = 0; c < ncomp; c++) {
+      auto v = SI::to_c(s[(int64_t)c * nrhs]);
+      m = fmax(m, fmax(fabs((double)v.x * si), fabs((double)v.y * si)));
+    }
+    dst_norm[(int64_t)site * nrhs + r] = (float)m;
+  }
+  const double inv = SO::has_norm ? (m > 0.0 ? 1.0 / (double)(float)m : 0.0) : 1.0;
+  for (int c = 0; c < ncomp; c++) {
+    auto v = SI::to_c(s[(int64_t)c * nrhs]);
+    const double re = (double)v.x * si * inv, im = (double)v.y * si * inv;
+    typename SO::elem e;
+    if constexpr (PO == PREC_DOUBLE) {
+      e = make_double2(re, im);
+    } else if constexpr (PO == PREC_SINGLE) {
+      e = make_float2((float)re, (float)im);
+    } else {
+      e = SO::from_c(make_float2((float)re, (float)im));
+    }
+    d[(int64_t)c * nrhs] = e;
+  }
+}
+
+template <int P>
+__global__ void convert_gauge_kernel(const double2* __restrict__ src, void* dst, int64_t count) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const double2 v = src[i];
+    E e;
+    if constexpr (P == PREC_DOUBLE) {
+      e = v;
+    } else if constexpr (P == PREC_SINGLE) {
+      e = make_float2((float)v.x, (float)v.y);
+    } else {
+      e = S::from_c(make_float2((float)v.x, (float)v.y));
+    }
+    static_cast<E*>(dst)[i] = e;
+  }
+}
+
+// [rows][cols] -> [cols][rows] complex double transpose through shared memory
+__global__ void transpose_c64_kernel(const double2* __restrict__ src, double2* __restrict__ dst, int rows, int cols) {
+  __shared__ double2 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + j, c = bx + threadIdx.x;
+    if (r < rows && c < cols) tile[j][threadIdx.x] = src[(int64_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int c = bx + j, r = by + threadIdx.x;
+    if (r < rows && c < cols) dst[(int64_t)c * rows + r] = tile[threadIdx.x][j];
+  }
+}
+
+template <int N>
+void pack_n(int prec, const PtrArray& src, int mode, int parity, void* dst, float* dst_norm, const Geometry& g,
+            int nrhs, cudaStream_t st) {
+  const int64_t threads = (int64_t)g.vh * nrhs;
+  const int block = 128;
+  const int grid = (int)((threads + block - 1) / block);
+  FastDiv dn((uint32_t)nrhs);
+  switch (prec) {
+    case PREC_DOUBLE: pack_fermions_kernel<PREC_DOUBLE, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
+    case PREC_SINGLE: pack_fermions_kernel<PREC_SINGLE, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
+    case PREC_HALF: pack_fermions_kernel<PREC_HALF, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
+    case PREC_BF16: pack_fermions_kernel<PREC_BF16, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
+  }
+}
+
+template <int N>
+void unpack_n(int prec, const PtrArray& dst, int mode, int parity, const void* src, const float* src_norm,
+              const Geometry& g, int nrhs, cudaStream_t st) {
+  const int64_t threads = (int64_t)g.vh * nrhs;
+  const int block = 128;
+  const int grid = (int)((threads + block - 1) / block);
+  FastDiv dn((uint32_t)nrhs);
+  switch (prec) {
+    case PREC_DOUBLE: unpack_fermions_kernel<PREC_DOUBLE, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
+    case PREC_SINGLE: unpack_fermions_kernel<PREC_SINGLE, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
+    case PREC_HALF: unpack_fermions_kernel<PREC_HALF, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
+    case PREC_BF16: unpack_fermions_kernel<PREC_BF16, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
+  }
+}
+
+}  // namespace
+
+void pack_fermions(int prec, int N, const PtrArray& src, int mode, int parity, void* dst, float* dst_norm,
+                   const Geometry& g, int nrhs, cudaStream_t st) {
+  QCU_REQUIRE(nrhs >= 1 && nrhs <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs out of range");
+  QCU_REQUIRE((int64_t)g.vh * nrhs < (1ll << 31), QCU_ERR_INVALID_ARGUMENT, "lattice x nrhs too large");
+  switch (N) {
+    case 3: pack_n<3>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    case 4: pack_n<4>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    case 5: pack_n<5>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    case 6: pack_n<6>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    case 7: pack_n<7>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    case 8: pack_n<8>(prec, src, mode, parity, dst, dst_norm, g, nrhs, st); break;
+    default: throw Error(QCU_ERR_UNSUPPORTED, "nColors must be in 3..8");
+  }
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void unpack_fermions(int prec, int N, const PtrArray& dst, int mode, int parity, const void* src,
+                     const float* src_norm, const Geometry& g, int nrhs, cudaStream_t st) {
+  QCU_REQUIRE(nrhs >= 1 && nrhs <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs out of range");
+  QCU_REQUIRE((int64_t)g.vh * nrhs < (1ll << 31), QCU_ERR_INVALID_ARGUMENT, "lattice x nrhs too large");
+  switch (N) {
+    case 3: unpack_n<3>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    case 4: unpack_n<4>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    case 5: unpack_n<5>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    case 6: unpack_n<6>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    case 7: unpack_n<7>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    case 8: unpack_n<8>(prec, dst, mode, parity, src, src_norm, g, nrhs, st); break;
+    default: throw Error(QCU_ERR_UNSUPPORTED, "nColors must be in 3..8");
+  }
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void pack_gauge(int prec, int N, const void* src, int lex, void* dst, const Geometry& g, cudaStream_t st) {
+  const int64_t threads = (int64_t)8 * g.vh;
+  const int block = 256;
+  const int grid = (int)((threads + block - 1) / block);
+  const double2* s = static_cast<const double2*>(src);
+  switch (prec) {
+    case PREC_DOUBLE: pack_gauge_kernel<PREC_DOUBLE><<<grid, block, 0, st>>>(s, lex, dst, g, N * N); break;
+    case PREC_SINGLE: pack_gauge_kernel<PREC_SINGLE><<<grid, block, 0, st>>>(s, lex, dst, g, N * N); break;
+    case PREC_HALF: pack_gauge_kernel<PREC_HALF><<<grid, block, 0, st>>>(s, lex, dst, g, N * N); break;
+    case PREC_BF16: pack_gauge_kernel<PREC_BF16><<<grid, block, 0, st>>>(s, lex, dst, g, N * N); break;
+    default: throw Error(QCU_ERR_UNSUPPORTED, "bad precision");
+  }
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void unpack_gauge_fp64(int N, const void* src, void* dst, const Geometry& g, cudaStream_t st) {
+  const int64_t threads = (int64_t)8 * g.vh;
+  const int block = 256;
+  const int grid = (int)((threads + block - 1) / block);
+  unpack_gauge_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src), static_cast<double2*>(dst), g.vh,
+                                              N * N);
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void convert_field(int prec_in, const void* src, const float* src_norm, int prec_out, void* dst, float* dst_norm,
+                   int64_t vh, int ncomp, int nrhs, cudaStream_t st) {
+  const int64_t threads = vh * nrhs;
+  QCU_REQUIRE(threads < (1ll << 31), QCU_ERR_INVALID_ARGUMENT, "field too large");
+  const int block = 256;
+  const int grid = (int)((threads + block - 1) / block);
+  FastDiv dn((uint32_t)nrhs);
+#define QCU_CONV(PI, PO)                                                                                       \
+  if (prec_in == PI && prec_out == PO) {                                                                       \
+    convert_field_kernel<PI, PO><<<grid, block, 0, st>>>(src, src_norm, dst, dst_norm, vh, ncomp, nrhs, dn);  \
+    QCU_CHECK_CUDA(cudaGetLastError());                                                                        \
+    return;                                                                                                    \
+  }
+  QCU_CONV(PREC_DOUBLE, PREC_SINGLE)
+  QCU_CONV(PREC_DOUBLE, PREC_HALF)
+  QCU_CONV(PREC_DOUBLE, PREC_BF16)
+  QCU_CONV(PREC_SINGLE, PREC_DOUBLE)
+  QCU_CONV(PREC_HALF, PREC_DOUBLE)
+  QCU_CONV(PREC_BF16, PREC_DOUBLE)
+  QCU_CONV(PREC_SINGLE, PREC_HALF)
+  QCU_CONV(PREC_SINGLE, PREC_BF16)
+  QCU_CONV(PREC_HALF, PREC_SINGLE)
+  QCU_CONV(PREC_BF16, PREC_SINGLE)
+  QCU_CONV(PREC_DOUBLE, PREC_DOUBLE)
+  QCU_CONV(PREC_SINGLE, PREC_SINGLE)
+  QCU_CONV(PREC_HALF, PREC_HALF)
+  QCU_CONV(PREC_BF16, PREC_BF16)
+#undef QCU_CONV
+  throw Error(QCU_ERR_UNSUPPORTED, "unsupported precision conversion");
+}
+
+void convert_gauge(const void* src_fp64, int prec, void* dst, int64_t count, cudaStream_t st) {
+  const int block = 256;
+  const int grid = (int)std::min<int64_t>((count + block - 1) / block, 152 * 32);
+  const double2* s = static_cast<const double2*>(src_fp64);
+  switch (prec) {
+    case PREC_DOUBLE: convert_gauge_kernel<PREC_DOUBLE><<<grid, block, 0, st>>>(s, dst, count); break;
+    case PREC_SINGLE: convert_gauge_kernel<PREC_SINGLE><<<grid, block, 0, st>>>(s, dst, count); break;
+    case PREC_HALF: convert_gauge_kernel<PREC_HALF><<<grid, block, 0, st>>>(s, dst, count); break;
+    case PREC_BF16: convert_gauge_kernel<PREC_BF16><<<grid, block, 0, st>>>(s, dst, count); break;
+    default: throw Error(QCU_ERR_UNSUPPORTED, "bad precision");
+  }
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st) {
+  dim3 block(32, 8);
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+  transpose_c64_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src), static_cast<double2*>(dst), rows,
+                                               cols);
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+}  // namespace qcu

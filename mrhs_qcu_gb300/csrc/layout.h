@@ -1,0 +1,41 @@
+// Host launchers of the layout-transform kernels (layout.cu).
+#pragma once
+
+#include "qcu_common.cuh"
+
+namespace qcu {
+
+constexpr int QCU_MAX_RHS = 256;
+
+// caller-side fermion address modes
+enum SrcMode : int {
+  SRC_EO_HALF = 0,  // pointer to one parity, [Vh][4][N]
+  SRC_EO_FULL = 1,  // pointer to [2][Vh][4][N]; the parity argument selects the half
+  SRC_LEX = 2,      // pointer to a lexicographic full field [V][4][N]
+};
+
+// one device pointer per RHS, passed by value as a kernel parameter
+struct PtrArray {
+  const void* p[QCU_MAX_RHS];
+};
+
+// caller FP64 fermions (nrhs pointers) -> internal MRHS field of `prec`
+void pack_fermions(int prec, int N, const PtrArray& src, int mode, int parity, void* dst, float* dst_norm,
+                   const Geometry& g, int nrhs, cudaStream_t st);
+// internal MRHS field -> caller FP64 fermions
+void unpack_fermions(int prec, int N, const PtrArray& dst, int mode, int parity, const void* src,
+                     const float* src_norm, const Geometry& g, int nrhs, cudaStream_t st);
+// caller FP64 gauge (eo [4][2][Vh][N][N], or lexicographic [4][V][N][N] when
+// lex != 0) -> internal [4][2][N*N][Vh] of `prec`
+void pack_gauge(int prec, int N, const void* src, int lex, void* dst, const Geometry& g, cudaStream_t st);
+// internal FP64 gauge -> caller eo layout
+void unpack_gauge_fp64(int N, const void* src, void* dst, const Geometry& g, cudaStream_t st);
+// MRHS field precision conversion (same [vh][ncomp][nrhs] layout)
+void convert_field(int prec_in, const void* src, const float* src_norm, int prec_out, void* dst, float* dst_norm,
+                   int64_t vh, int ncomp, int nrhs, cudaStream_t st);
+// FP64 internal gauge -> the same layout in `prec` (no scales: |U_ab| <= 1)
+void convert_gauge(const void* src_fp64, int prec, void* dst, int64_t count, cudaStream_t st);
+// plain complex-double transpose [rows][cols] -> [cols][rows]
+void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st);
+
+}  // namespace qcu

@@ -1,0 +1,434 @@
+// C ABI of libqcu.so: the reference's qcu.h entry points (src/qcu.cu:125-181
+// of the reference) plus the extensions in qcu_gb300.h.
+//
+// The reference keeps one global Qcu object (src/qcu.cu:125); so does this
+// library (g_session), guarded by a mutex.  Errors are recorded and printed
+// instead of terminating the process (the reference's errorQcu / CHECK_CUDA
+// call exit(1), include/qcu_macro.cuh:16-40); QCU_ABORT_ON_ERROR=1 restores
+// that behaviour.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+
+#include "../../include/qcu.h"
+#include "../../include/qcu_gb300.h"
+#include "session.h"
+
+using qcu::Error;
+using qcu::Session;
+
+namespace {
+
+std::mutex g_mutex;
+std::unique_ptr<Session> g_session;
+std::unique_ptr<Session> g_solver_session;  // private session of cg_inverter
+cudaStream_t g_user_stream = nullptr;
+int g_antiperiodic = 0;
+thread_local int g_last_error = 0;
+thread_local std::string g_last_message;
+
+void record(int code, const std::string& msg) {
+  g_last_error = code;
+  g_last_message = msg;
+  fprintf(stderr, "%s", msg.c_str());
+  if (msg.empty() || msg.back() != '\n') fprintf(stderr, "\n");
+  fprintf(stderr, "Error happened in libqcu (code %d)\n", code);
+  const char* e = getenv("QCU_ABORT_ON_ERROR");
+  if (e && e[0] == '1') exit(1);
+}
+
+template <typename F>
+int guarded(F&& f) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  try {
+    f();
+    return QCU_OK;
+  } catch (const Error& e) {
+    record(e.code, e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    record(QCU_ERR_OUT_OF_MEMORY, "host allocation failed");
+    return QCU_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    record(QCU_ERR_CUDA, e.what());
+    return QCU_ERR_CUDA;
+  }
+}
+
+Session& session() {
+  QCU_REQUIRE(g_session != nullptr, QCU_ERR_NOT_INITIALIZED, "Qcu is not initialized.\n");
+  return *g_session;
+}
+
+void check_lattice(const QcuParam* p) {
+  QCU_REQUIRE(p != nullptr, QCU_ERR_INVALID_ARGUMENT, "QcuParam is null");
+  for (int i = 0; i < 4; i++)
+    QCU_REQUIRE(p->lattice_size[i] > 0, QCU_ERR_INVALID_ARGUMENT, "lattice sizes must be positive");
+  QCU_REQUIRE(p->lattice_size[0] % 2 == 0, QCU_ERR_INVALID_ARGUMENT, "lattice X extent must be even");
+  const long long v = (long long)p->lattice_size[0] * p->lattice_size[1] * p->lattice_size[2] * p->lattice_size[3];
+  QCU_REQUIRE(v / 2 < (1ll << 30), QCU_ERR_INVALID_ARGUMENT, "lattice too large");
+}
+
+void apply_settings(Session& s) {
+  s.antiperiodic_t = g_antiperiodic != 0;
+  s.set_user_stream(g_user_stream);
+}
+
+// run the hopping term on caller-layout fermions through the session
+void caller_dslash(Session& s, int prec, void* const* outs, void* const* ins, int n, int in_mode, int out_mode,
+                   int parity, int dagger) {
+  using namespace qcu;
+  for (int base = 0; base < n; base += QCU_MAX_RHS) {
+    const int m = std::min(QCU_MAX_RHS, n - base);
+    PtrArray pin{}, pout{};
+    for (int r = 0; r < m; r++) {
+      pin.p[r] = ins[base + r];
+      pout.p[r] = outs[base + r];
+    }
+    FieldView fin = s.alloc_field("abi.in", prec, m);
+    FieldView fout = s.alloc_field("abi.out", prec, m);
+    pack_fermions(prec, s.N, pin, in_mode, 1 - parity, fin.data, fin.norm, s.geo, m, s.stream());
+    s.hop(fout, fin, FieldView{}, parity, dagger, 1.0, 0.0);
+    unpack_fermions(prec, s.N, pout, out_mode, parity, fout.data, fout.norm, s.geo, m, s.stream());
+  }
+  s.sync();
+}
+
+}  // namespace
+
+extern "C" {
+
+// used by the C++ storage API (storage_api.cu) to report through the same channel
+void qcu_record_error(int code, const char* msg) {
+  std::lock_guard<std::mutex> lk(g_mutex);
+  record(code, msg);
+}
+
+// ---- drop-in ABI (include/qcu.h) -------------------------------------------
+void initGridSize(QcuGrid_t* grid, QcuParam* p_param, int nColors) {
+  guarded([&] {
+    check_lattice(p_param);
+    QCU_REQUIRE(nColors >= 3 && nColors <= 8, QCU_ERR_UNSUPPORTED, "Now we only support 3-8 colors.\n");
+    int g[4] = {1, 1, 1, 1};
+    if (grid)
+      for (int i = 0; i < 4; i++) g[i] = grid->grid_size[i];
+    for (int i = 0; i < 4; i++)
+      QCU_REQUIRE(g[i] == 1, QCU_ERR_UNSUPPORTED,
+                  "process grids other than 1x1x1x1 are not supported (one GPU per process)");
+    g_session.reset();
+    g_session.reset(new Session(p_param->lattice_size, g, nColors));
+    apply_settings(*g_session);
+  });
+}
+
+void pushBackFermions(void* fermionOut, void* fermionIn) {
+  guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(fermionOut && fermionIn, QCU_ERR_INVALID_ARGUMENT, "fermion pointers must not be null");
+    s.queue.emplace_back(fermionOut, fermionIn);
+  });
+}
+
+void startDslash(int parity, int daggerFlag) {
+  guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(s.dirac != nullptr, QCU_ERR_NO_OPERATOR, "getDslash has not been called");
+    QCU_REQUIRE(parity == 0 || parity == 1, QCU_ERR_INVALID_ARGUMENT, "parity must be 0 or 1");
+    QCU_REQUIRE(daggerFlag == 0 || daggerFlag == 1, QCU_ERR_INVALID_ARGUMENT, "daggerFlag must be 0 or 1");
+    std::vector<void*> outs, ins;
+    for (auto& pr : s.queue) {
+      outs.push_back(pr.first);
+      ins.push_back(pr.second);
+    }
+    s.queue.clear();
+    if (outs.empty()) return;
+    caller_dslash(s, s.dirac->precision(), outs.data(), ins.data(), (int)outs.size(), qcu::SRC_EO_HALF,
+                  qcu::SRC_EO_HALF, parity, daggerFlag);
+  });
+}
+
+void loadQcuGauge(void* gauge) {
+  guarded([&] {
+    Session& s = session();
+    s.load_gauge(gauge, 0);
+    s.sync();
+  });
+}
+
+void getDslash(int dslashType, double mass, int nColors, int nInputs, int floatPrecision) {
+  guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(s.gauge_loaded(), QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
+    QCU_REQUIRE(dslashType == 0, QCU_ERR_UNSUPPORTED, "Now we only support Wilson dslash.\n");
+    QCU_REQUIRE(nColors == s.N, QCU_ERR_INVALID_ARGUMENT, "nColors differs from initGridSize");
+    QCU_REQUIRE(qcu::prec_valid(floatPrecision), QCU_ERR_UNSUPPORTED,
+                "floatPrecision must be 0 (half), 1 (single), 2 (double) or 4 (bf16)");
+    QCU_REQUIRE(nInputs >= 0, QCU_ERR_INVALID_ARGUMENT, "nInputs must not be negative");
+    s.dirac.reset(new qcu::DiracWilson(s, mass, nColors, floatPrecision, dslashType));
+    s.gauge(floatPrecision);  // convert the resident gauge once
+    s.sync();
+  });
+}
+
+void dslashQcu(void* fermion_out, void* fermion_in, void* gauge, QcuParam* param, int parity) {
+  guarded([&] {
+    check_lattice(param);
+    QCU_REQUIRE(fermion_out && fermion_in && gauge, QCU_ERR_INVALID_ARGUMENT, "null pointer");
+    int g[4] = {1, 1, 1, 1};
+    Session s(param->lattice_size, g, 3);
+    apply_settings(s);
+    s.load_gauge(gauge, 0);
+    caller_dslash(s, qcu::PREC_DOUBLE, &fermion_out, &fermion_in, 1, qcu::SRC_EO_HALF, qcu::SRC_EO_HALF, parity, 0);
+  });
+}
+
+void fullDslashQcu(void* fermion_out, void* fermion_in, void* gauge, QcuParam* param, int dagger_flag) {
+  guarded([&] {
+    check_lattice(param);
+    QCU_REQUIRE(fermion_out && fermion_in && gauge, QCU_ERR_INVALID_ARGUMENT, "null pointer");
+    int g[4] = {1, 1, 1, 1};
+    Session s(param->lattice_size, g, 3);
+    apply_settings(s);
+    s.load_gauge(gauge, 0);
+    for (int p = 0; p < 2; p++)
+      caller_dslash(s, qcu::PREC_DOUBLE, &fermion_out, &fermion_in, 1, qcu::SRC_EO_FULL, qcu::SRC_EO_FULL, p,
+                    dagger_flag);
+  });
+}
+
+void cg_inverter(void* x_vector, void* b_vector, void* gauge, QcuParam* param, double p_max_prec, double p_kappa) {
+  guarded([&] {
+    check_lattice(param);
+    QCU_REQUIRE(x_vector && b_vector && gauge, QCU_ERR_INVALID_ARGUMENT, "null pointer");
+    const int N = g_session ? g_session->N : 3;
+    bool reuse = g_solver_session && g_solver_session->N == N;
+    for (int i = 0; reuse && i < 4; i++) reuse = g_solver_session->latt.dim[i] == param->lattice_size[i];
+    if (!reuse) {
+      int g[4] = {1, 1, 1, 1};
+      g_solver_session.reset(new Session(param->lattice_size, g, N));
+    }
+    Session& s = *g_solver_session;
+    apply_settings(s);
+    s.load_gauge(gauge, 0);
+    qcu::SolveRequest q;
+    q.kappa = p_kappa;
+    q.tol = p_max_prec;
+    q.inner_prec = qcu::PREC_SINGLE;
+    q.src_mode = qcu::SRC_EO_FULL;
+    qcu::SolveResult r = qcu::solve(s, &x_vector, &b_vector, 1, q);
+    QCU_REQUIRE(r.converged[0], QCU_ERR_NOT_CONVERGED,
+                "cg_inverter: not converged, true residual " + std::to_string(r.true_residual[0]));
+  });
+}
+
+// ---- extensions (include/qcu_gb300.h) --------------------------------------
+int qcuGetLastError(void) { return g_last_error; }
+const char* qcuGetLastErrorString(void) { return g_last_message.c_str(); }
+void qcuClearError(void) {
+  g_last_error = 0;
+  g_last_message.clear();
+}
+const char* qcuVersion(void) { return "mrhs_qcu_gb300 0.1 (sm_103a)"; }
+
+int qcuSetAntiperiodicT(int flag) {
+  return guarded([&] {
+    g_antiperiodic = flag ? 1 : 0;
+    if (g_session) g_session->antiperiodic_t = g_antiperiodic != 0;
+  });
+}
+
+int qcuSetStream(void* stream) {
+  return guarded([&] {
+    g_user_stream = static_cast<cudaStream_t>(stream);
+    if (g_session) g_session->set_user_stream(g_user_stream);
+  });
+}
+
+int qcuSynchronize(void) {
+  return guarded([&] { session().sync(); });
+}
+
+int qcuFieldBytes(int precision, int nrhs, size_t* data_bytes, size_t* norm_bytes) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    QCU_REQUIRE(nrhs >= 1, QCU_ERR_INVALID_ARGUMENT, "nrhs must be positive");
+    if (data_bytes) *data_bytes = s.field_bytes(precision, nrhs);
+    if (norm_bytes) *norm_bytes = s.norm_bytes(precision, nrhs);
+  });
+}
+
+int qcuPackFermions(void* dst, void* dst_norm, void* const* src, int nrhs, int src_mode, int parity, int precision) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(nrhs >= 1 && nrhs <= qcu::QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
+    QCU_REQUIRE(src_mode >= 0 && src_mode <= 2, QCU_ERR_INVALID_ARGUMENT, "bad source mode");
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    QCU_REQUIRE(!qcu::prec_is16(precision) || dst_norm, QCU_ERR_INVALID_ARGUMENT, "16-bit fields need a norm array");
+    qcu::PtrArray p{};
+    for (int r = 0; r < nrhs; r++) p.p[r] = src[r];
+    qcu::pack_fermions(precision, s.N, p, src_mode, parity, dst, static_cast<float*>(dst_norm), s.geo, nrhs,
+                       s.stream());
+  });
+}
+
+int qcuUnpackFermions(void* const* dst, const void* src, const void* src_norm, int nrhs, int dst_mode, int parity,
+                      int precision) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(nrhs >= 1 && nrhs <= qcu::QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
+    QCU_REQUIRE(dst_mode >= 0 && dst_mode <= 2, QCU_ERR_INVALID_ARGUMENT, "bad destination mode");
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    qcu::PtrArray p{};
+    for (int r = 0; r < nrhs; r++) p.p[r] = dst[r];
+    qcu::unpack_fermions(precision, s.N, p, dst_mode, parity, src, static_cast<const float*>(src_norm), s.geo, nrhs,
+                         s.stream());
+  });
+}
+
+int qcuLoadGaugeLex(void* gauge_lex) {
+  return guarded([&] {
+    Session& s = session();
+    s.load_gauge(gauge_lex, 1);
+    s.sync();
+  });
+}
+
+int qcuLexToEo(void* eo_out, const void* lex_in, int ncomp) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(ncomp == 4 * s.N, QCU_ERR_UNSUPPORTED, "ncomp must be 4*N (a fermion field)");
+    qcu::PtrArray src{}, dst{};
+    src.p[0] = lex_in;
+    dst.p[0] = eo_out;
+    qcu::FieldView f = s.alloc_field("lex.tmp", qcu::PREC_DOUBLE, 1);
+    for (int p = 0; p < 2; p++) {
+      qcu::pack_fermions(qcu::PREC_DOUBLE, s.N, src, qcu::SRC_LEX, p, f.data, nullptr, s.geo, 1, s.stream());
+      qcu::unpack_fermions(qcu::PREC_DOUBLE, s.N, dst, qcu::SRC_EO_FULL, p, f.data, nullptr, s.geo, 1, s.stream());
+    }
+    s.sync();
+  });
+}
+
+int qcuEoToLex(void* lex_out, const void* eo_in, int ncomp) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(ncomp == 4 * s.N, QCU_ERR_UNSUPPORTED, "ncomp must be 4*N (a fermion field)");
+    qcu::PtrArray src{}, dst{};
+    src.p[0] = eo_in;
+    dst.p[0] = lex_out;
+    qcu::FieldView f = s.alloc_field("lex.tmp", qcu::PREC_DOUBLE, 1);
+    for (int p = 0; p < 2; p++) {
+      qcu::pack_fermions(qcu::PREC_DOUBLE, s.N, src, qcu::SRC_EO_FULL, p, f.data, nullptr, s.geo, 1, s.stream());
+      qcu::unpack_fermions(qcu::PREC_DOUBLE, s.N, dst, qcu::SRC_LEX, p, f.data, nullptr, s.geo, 1, s.stream());
+    }
+    s.sync();
+  });
+}
+
+int qcuDslashMRHS(void* out, void* out_norm, const void* in, const void* in_norm, int nrhs, int parity, int dagger,
+                  int precision) {
+  return qcuDslashXpayMRHS(out, out_norm, in, in_norm, nullptr, nullptr, nrhs, parity, dagger, precision, 1.0, 0.0);
+}
+
+int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_norm, const void* x,
+                      const void* x_norm, int nrhs, int parity, int dagger, int precision, double a, double b) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    QCU_REQUIRE(nrhs >= 1, QCU_ERR_INVALID_ARGUMENT, "nrhs must be positive");
+    QCU_REQUIRE(out && in, QCU_ERR_INVALID_ARGUMENT, "null field");
+    QCU_REQUIRE(out != in, QCU_ERR_INVALID_ARGUMENT, "in-place dslash is not supported");
+    QCU_REQUIRE(((uintptr_t)out | (uintptr_t)in | (uintptr_t)x) % 16 == 0, QCU_ERR_INVALID_ARGUMENT,
+                "fields must be 16-byte aligned");
+    const bool h = qcu::prec_is16(precision);
+    QCU_REQUIRE(!h || (out_norm && in_norm && (!x || x_norm)), QCU_ERR_INVALID_ARGUMENT,
+                "16-bit fields need norm arrays");
+    qcu::FieldView fo, fi, fx;
+    fo.data = out;
+    fo.norm = static_cast<float*>(out_norm);
+    fi.data = const_cast<void*>(in);
+    fi.norm = static_cast<float*>(const_cast<void*>(in_norm));
+    fx.data = const_cast<void*>(x);
+    fx.norm = static_cast<float*>(const_cast<void*>(x_norm));
+    fo.prec = fi.prec = fx.prec = precision;
+    fo.nrhs = fi.nrhs = fx.nrhs = nrhs;
+    s.hop(fo, fi, fx, parity, dagger, a, b);
+  });
+}
+
+int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    qcu::FieldView fi = s.alloc_field("tune.in", precision, nrhs);
+    qcu::FieldView fo = s.alloc_field("tune.out", precision, nrhs);
+    QCU_CHECK_CUDA(cudaMemsetAsync(fi.data, 0, s.field_bytes(precision, nrhs), s.stream()));
+    if (fi.norm) QCU_CHECK_CUDA(cudaMemsetAsync(fi.norm, 0, s.norm_bytes(precision, nrhs), s.stream()));
+    qcu::DslashArgs A;
+    A.gauge = s.gauge(precision);
+    A.in = fi.data;
+    A.in_norm = fi.norm;
+    A.out = fo.data;
+    A.out_norm = fo.norm;
+    A.x = nullptr;
+    A.x_norm = nullptr;
+    A.mask = nullptr;
+    A.a = 1.0;
+    A.b = 0.0;
+    A.geo = s.geo;
+    A.nrhs = nrhs;
+    A.parity = 0;
+    A.dagger = 0;
+    A.antiperiodic_t = 0;
+    qcu::DslashConfig c = s.tuner.tune(A, precision, s.N, s.stream());
+    if (rhs_per_thread) *rhs_per_thread = c.R;
+    if (block) *block = c.block;
+  });
+}
+
+void qcuSolverParamDefaults(QcuSolverParam* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->solver = QCU_SOLVER_CG;
+  p->inner_precision = QCU_SINGLE_PRECISION;
+  p->kappa = 0.125;
+  p->tol = 1e-10;
+  p->max_iter = 10000;
+  p->delta = 0.1;
+  p->use_graph = 1;
+  p->src_mode = QCU_SRC_EO_FULL;
+}
+
+int qcuInvert(void* const* x, void* const* b, int nrhs, QcuSolverParam* p) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(p != nullptr, QCU_ERR_INVALID_ARGUMENT, "null solver parameters");
+    QCU_REQUIRE(x && b, QCU_ERR_INVALID_ARGUMENT, "null field arrays");
+    qcu::SolveRequest q;
+    q.solver = p->solver;
+    q.inner_prec = p->inner_precision;
+    q.kappa = p->kappa;
+    q.tol = p->tol;
+    q.max_iter = p->max_iter;
+    q.delta = p->delta > 0 ? p->delta : 0.1;
+    q.use_graph = p->use_graph != 0;
+    q.src_mode = p->src_mode;
+    qcu::SolveResult r = qcu::solve(s, x, b, nrhs, q);
+    p->iterations = r.iterations;
+    p->reliable_updates = r.reliable_updates;
+    p->seconds = r.seconds;
+    bool all = true;
+    for (int i = 0; i < nrhs && i < 256; i++) {
+      p->true_residual[i] = r.true_residual[i];
+      p->converged[i] = r.converged[i];
+      all &= r.converged[i] != 0;
+    }
+    QCU_REQUIRE(all, QCU_ERR_NOT_CONVERGED, "qcuInvert: not every RHS converged");
+  });
+}
+
+}  // extern "C"

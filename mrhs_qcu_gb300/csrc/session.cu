@@ -1,0 +1,249 @@
+// Session, Dirac and autotuner implementation (see session.h).
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <sstream>
+
+#include "session.h"
+
+namespace qcu {
+
+// ---------------------------------------------------------------------------
+void* DeviceBuffer::ensure(size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes > bytes_) {
+    release();
+    QCU_CHECK_CUDA(cudaMalloc(&p_, bytes));
+    bytes_ = bytes;
+  }
+  return p_;
+}
+
+void DeviceBuffer::release() {
+  if (p_) cudaFree(p_);
+  p_ = nullptr;
+  bytes_ = 0;
+}
+
+size_t Workspace::total_bytes() const {
+  size_t s = 0;
+  for (auto& kv : bufs_) s += kv.second.bytes();
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+Autotuner& global_tuner() {
+  static Autotuner t;
+  return t;
+}
+
+bool Autotuner::enabled() const {
+  const char* e = getenv("QCU_TUNE");
+  return !(e && e[0] == '0');
+}
+
+std::string Autotuner::key(int prec, int N, int nrhs, int vh) const {
+  std::ostringstream o;
+  o << prec << ":" << N << ":" << nrhs << ":" << vh;
+  return o.str();
+}
+
+void Autotuner::load_file() {
+  file_loaded_ = true;
+  const char* path = getenv("QCU_TUNE_CACHE");
+  if (!path) return;
+  std::ifstream in(path);
+  std::string k;
+  int R, block;
+  while (in >> k >> R >> block) {
+    DslashConfig c;
+    c.R = R;
+    c.block = block;
+    cache_[k] = c;
+  }
+}
+
+void Autotuner::save_file() {
+  const char* path = getenv("QCU_TUNE_CACHE");
+  if (!path) return;
+  std::ofstream out(path);
+  for (auto& kv : cache_) out << kv.first << " " << kv.second.R << " " << kv.second.block << "\n";
+}
+
+DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
+  std::lock_guard<std::mutex> lk(m_);
+  if (!file_loaded_) load_file();
+  auto it = cache_.find(key(prec, N, nrhs, vh));
+  *found = it != cache_.end();
+  return *found ? it->second : heuristic(prec, N, nrhs);
+}
+
+void Autotuner::store(int prec, int N, int nrhs, int vh, const DslashConfig& c) {
+  std::lock_guard<std::mutex> lk(m_);
+  cache_[key(prec, N, nrhs, vh)] = c;
+  save_file();
+}
+
+DslashConfig Autotuner::heuristic(int prec, int N, int nrhs) {
+  DslashConfig c;
+  int opts[8];
+  const int n = dslash_r_options(prec, N, opts, 8);
+  int want = prec == PREC_DOUBLE ? 1 : (prec == PREC_SINGLE ? 2 : 4);
+  if (N > 4) want = 1;
+  c.R = 1;
+  for (int i = 0; i < n; i++)
+    if (opts[i] <= want && nrhs % opts[i] == 0) {
+      c.R = opts[i];
+      break;
+    }
+  c.block = 128;
+  return c;
+}
+
+DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t st) {
+  int opts[8];
+  const int n = dslash_r_options(prec, N, opts, 8);
+  const int blocks[] = {64, 128, 256};
+  cudaEvent_t e0, e1;
+  QCU_CHECK_CUDA(cudaEventCreate(&e0));
+  QCU_CHECK_CUDA(cudaEventCreate(&e1));
+  DslashConfig best = heuristic(prec, N, A.nrhs);
+  float best_ms = 1e30f;
+  for (int i = 0; i < n; i++) {
+    if (A.nrhs % opts[i]) continue;
+    for (int b : blocks) {
+      DslashConfig c;
+      c.R = opts[i];
+      c.block = b;
+      launch_dslash(A, prec, N, c, st);  // warm-up
+      QCU_CHECK_CUDA(cudaEventRecord(e0, st));
+      const int reps = 3;
+      for (int k = 0; k < reps; k++) launch_dslash(A, prec, N, c, st);
+      QCU_CHECK_CUDA(cudaEventRecord(e1, st));
+      QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  store(prec, N, A.nrhs, A.geo.vh, best);
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+void DiracWilson::Dslash(FieldView out, FieldView in, int parity, int dagger, int nInputs) {
+  QCU_REQUIRE(out.nrhs == nInputs && in.nrhs == nInputs, QCU_ERR_INVALID_ARGUMENT, "Dslash: nInputs mismatch");
+  s_.hop(out, in, FieldView{}, parity, dagger, 1.0, 0.0);
+}
+
+void DiracWilson::DslashXpay(FieldView out, FieldView in, FieldView x, int parity, int dagger, int nInputs, double a,
+                             double b) {
+  QCU_REQUIRE(out.nrhs == nInputs && in.nrhs == nInputs && x.nrhs == nInputs, QCU_ERR_INVALID_ARGUMENT,
+              "DslashXpay: nInputs mismatch");
+  s_.hop(out, in, x, parity, dagger, a, b);
+}
+
+// ---------------------------------------------------------------------------
+Session::Session(const int L[4], const int grid[4], int nColors) : tuner(global_tuner()) {
+  for (int i = 0; i < 4; i++) {
+    latt.dim[i] = L[i];
+    proc.dim[i] = grid ? grid[i] : 1;
+  }
+  N = nColors;
+  geo = make_geometry(L);
+}
+
+Session::~Session() {
+  if (own_stream_) cudaStreamDestroy(own_stream_);
+}
+
+cudaStream_t Session::stream() {
+  if (user_stream_) return user_stream_;
+  if (!own_stream_) QCU_CHECK_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamDefault));
+  return own_stream_;
+}
+
+void Session::sync() { QCU_CHECK_CUDA(cudaStreamSynchronize(stream())); }
+
+void Session::load_gauge(const void* caller_gauge, int lex) {
+  QCU_REQUIRE(caller_gauge != nullptr, QCU_ERR_INVALID_ARGUMENT, "gauge pointer is null");
+  const size_t bytes = (size_t)8 * geo.vh * N * N * 16;
+  void* d = gauge_[PREC_DOUBLE].ensure(bytes);
+  pack_gauge(PREC_DOUBLE, N, caller_gauge, lex, d, geo, stream());
+  for (int p = 0; p < 5; p++) gauge_valid_[p] = false;
+  gauge_valid_[PREC_DOUBLE] = true;
+  gauge_loaded_ = true;
+}
+
+const void* Session::gauge(int prec) {
+  QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
+  QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  if (!gauge_valid_[prec]) {
+    const int64_t count = (int64_t)8 * geo.vh * N * N;
+    void* d = gauge_[prec].ensure((size_t)count * prec_complex_bytes(prec));
+    // links are bounded by 1 in modulus, so 16-bit links carry no scale
+    convert_gauge(gauge_[PREC_DOUBLE].get(), prec, d, count, stream());
+    gauge_valid_[prec] = true;
+  }
+  return gauge_[prec].get();
+}
+
+FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {
+  FieldView f;
+  f.prec = prec;
+  f.nrhs = nrhs;
+  f.data = ws.get(name, field_bytes(prec, nrhs));
+  if (prec_is16(prec)) f.norm = static_cast<float*>(ws.get(name + ".norm", norm_bytes(prec, nrhs)));
+  return f;
+}
+
+void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagger, double a, double b,
+                  const int* mask) {
+  QCU_REQUIRE(parity == 0 || parity == 1, QCU_ERR_INVALID_ARGUMENT, "parity must be 0 or 1");
+  QCU_REQUIRE(dagger == 0 || dagger == 1, QCU_ERR_INVALID_ARGUMENT, "daggerFlag must be 0 or 1");
+  QCU_REQUIRE(out.prec == in.prec && (!x.data || x.prec == in.prec), QCU_ERR_INVALID_ARGUMENT,
+              "dslash operands must share one precision");
+  QCU_REQUIRE(out.nrhs == in.nrhs && (!x.data || x.nrhs == in.nrhs), QCU_ERR_INVALID_ARGUMENT,
+              "dslash operands must share nrhs");
+  DslashArgs A;
+  A.gauge = gauge(in.prec);
+  A.in = in.data;
+  A.in_norm = in.norm;
+  A.out = out.data;
+  A.out_norm = out.norm;
+  A.x = x.data;
+  A.x_norm = x.norm;
+  A.mask = mask;
+  A.a = a;
+  A.b = b;
+  A.geo = geo;
+  A.nrhs = in.nrhs;
+  A.parity = parity;
+  A.dagger = dagger;
+  A.antiperiodic_t = antiperiodic_t ? 1 : 0;
+  bool found = false;
+  DslashConfig c = tuner.lookup(in.prec, N, in.nrhs, geo.vh, &found);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  QCU_CHECK_CUDA(cudaStreamIsCapturing(stream(), &cs));
+  if (!found && tuner.enabled() && cs == cudaStreamCaptureStatusNone) c = tuner.tune(A, in.prec, N, stream());
+  launch_dslash(A, in.prec, N, c, stream());
+}
+
+Blas& Session::blas() {
+  if (!blas_) {
+    const int max_blocks = 1024;
+    double* p = static_cast<double*>(partials_.ensure((size_t)max_blocks * QCU_MAX_RHS * 2 * sizeof(double)));
+    blas_.reset(new Blas(p, max_blocks));
+  }
+  return *blas_;
+}
+
+double* Session::scalars(size_t count) { return static_cast<double*>(scalars_.ensure(count * sizeof(double))); }
+
+}  // namespace qcu

@@ -1,0 +1,227 @@
+"""GPU parity of the MRHS Wilson dslash through the C ABI (qcu.h), against
+the FP64 oracle, the reference kernel's golden outputs and, when
+oracle/_ref/ is present, the reference kernel itself on the same inputs.
+
+Tolerances (relative L2): 1e-13 FP64, 1e-6 FP32, 5e-3 FP16/BF16 storage."""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+from mrhs_qcu_gb300 import synthetic as S
+from oracle import oracle as O
+from tests.util import TOL, abi_dslash, dev, rel
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("prec", [2, 1, 0, 4])
+def test_config0_eo_oe_antiperiodic(cuda, qcu_lib, prec):
+    """8^4 SU(3) nrhs=4, antiperiodic t: D_eo and D_oe once each, both dagger flags."""
+    L = (8, 8, 8, 8)
+    g = S.random_gauge(L, 3, seed=31)
+    psi = S.random_fermions(L, 3, 4, seed=32)
+    for parity in (0, 1):
+        for dag in (0, 1):
+            got = abi_dslash(cuda, qcu_lib, psi, g, L, parity, dag, prec, antiperiodic_t=True)
+            ref = O.dslash(psi, g, L, parity, dag, True)
+            assert rel(got, ref) < TOL[prec], (parity, dag)
+
+
+def test_golden_reference_outputs(cuda, qcu_lib):
+    """Against the reference kernel's stored outputs (bitwise-identical inputs)."""
+    m = json.load(open(os.path.join(GOLDEN, "manifest.json")))
+    case = [c for c in m["cases"] if c["name"] == "su3_d_4x4x4x8_full"][0]
+    data = np.load(os.path.join(GOLDEN, case["file"]))
+    for c in case["combos"]:
+        got = abi_dslash(cuda, qcu_lib, data["psi"], data["gauge"], tuple(case["L"]), c["parity"], c["dagger"], 2,
+                         c["antiperiodic_t"])
+        assert rel(got, data[c["key"]]) < 1e-13
+
+
+@pytest.mark.parametrize("n,nrhs", [(3, 1), (3, 2), (3, 3), (3, 5), (3, 12), (3, 24), (4, 2), (4, 16), (5, 1),
+                                    (6, 2), (7, 1), (8, 2), (8, 4)])
+@pytest.mark.parametrize("prec", [2, 1])
+def test_colours_and_rhs_counts(cuda, qcu_lib, n, nrhs, prec):
+    L = (4, 4, 4, 4)
+    g = S.random_gauge(L, n, seed=40 + n)
+    psi = S.random_fermions(L, n, nrhs, seed=50 + nrhs)
+    got = abi_dslash(cuda, qcu_lib, psi, g, L, 1, 0, prec, antiperiodic_t=True)
+    assert rel(got, O.dslash(psi, g, L, 1, 0, True)) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", [0, 4])
+@pytest.mark.parametrize("n,nrhs", [(3, 4), (3, 12), (4, 8), (8, 2)])
+def test_half_storage(cuda, qcu_lib, prec, n, nrhs):
+    L = (4, 4, 4, 8)
+    g = S.random_gauge(L, n, seed=60 + n)
+    psi = S.random_fermions(L, n, nrhs, seed=61)
+    got = abi_dslash(cuda, qcu_lib, psi, g, L, 0, 1, prec)
+    assert rel(got, O.dslash(psi, g, L, 0, 1)) < TOL[prec]
+
+
+@pytest.mark.parametrize("L", [(6, 4, 4, 4), (2, 2, 2, 2), (4, 6, 2, 10), (12, 2, 4, 6)])
+def test_odd_and_tiny_lattices(cuda, qcu_lib, L):
+    """Half volumes that are not multiples of the block size (the reference
+    kernel has no tail guard) and odd half-X extents."""
+    g = S.random_gauge(L, 3, seed=70)
+    psi = S.random_fermions(L, 3, 3, seed=71)
+    for prec in (2, 1):
+        got = abi_dslash(cuda, qcu_lib, psi, g, L, 0, 0, prec, antiperiodic_t=True)
+        assert rel(got, O.dslash(psi, g, L, 0, 0, True)) < TOL[prec]
+
+
+def test_against_reference_kernel_same_inputs(cuda, qcu_lib):
+    from oracle import ref_runner
+    if not ref_runner.available():
+        pytest.skip("reference module not built (oracle/build_ref.sh)")
+    ref = ref_runner.RefModule()
+    for L, n, nrhs, prec in [((8, 8, 8, 8), 3, 4, "d"), ((8, 4, 4, 8), 3, 5, "d"), ((4, 4, 4, 8), 4, 2, "d"),
+                             ((8, 8, 8, 8), 3, 4, "f"), ((4, 4, 4, 8), 5, 1, "f")]:
+        g = S.random_gauge(L, n, seed=80)
+        psi = S.random_fermions(L, n, nrhs, seed=81)
+        for parity, dag, ap in [(0, 0, False), (1, 1, True)]:
+            r = ref.dslash(psi, g, L, parity, dag, prec, ap)
+            ours = abi_dslash(cuda, qcu_lib, psi, g, L, parity, dag, 2 if prec == "d" else 1, ap)
+            assert rel(ours, r) < (1e-13 if prec == "d" else 2e-6)
+
+
+def test_mrhs_equals_single_rhs(cuda, qcu_lib):
+    """Batching is exact: the 12-RHS result equals 12 one-RHS calls bitwise (FP64)."""
+    L = (8, 4, 4, 8)
+    g = S.random_gauge(L, 3, seed=90)
+    psi = S.random_fermions(L, 3, 12, seed=91)
+    batch = abi_dslash(cuda, qcu_lib, psi, g, L, 1, 0, 2)
+    for r in (0, 5, 11):
+        one = abi_dslash(cuda, qcu_lib, psi[r:r + 1], g, L, 1, 0, 2)
+        assert np.array_equal(one[0], batch[r])
+
+
+@pytest.mark.parametrize("prec", [2, 1, 0, 4])
+def test_resident_mrhs_api_and_xpay(cuda, qcu_lib, prec):
+    """qcuPackFermions -> qcuDslashXpayMRHS -> qcuUnpackFermions, lexicographic input."""
+    torch, Q = cuda, qcu_lib
+    L = (4, 4, 4, 8)
+    n, nrhs = 3, 6
+    g = S.random_gauge(L, n, seed=100)
+    full = S.random_fermions(L, n, nrhs, seed=101, parities=2)       # (nrhs, 2, Vh, 4, n)
+    lex = np.stack([O.eo_to_lex(full[r], L) for r in range(nrhs)])  # (nrhs, V, 4, n)
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    dg = dev(torch, g)
+    Q.loadQcuGauge(dg.data_ptr())
+    db, nb = Q.field_bytes(prec, nrhs)
+    bufs = [torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda") for _ in range(3)]
+    norms = [torch.empty(max(nb, 16) // 4, dtype=torch.float32, device="cuda") for _ in range(3)]
+    nrm = (lambda i: norms[i].data_ptr()) if nb else (lambda i: None)
+    src = [dev(torch, lex[r]) for r in range(nrhs)]
+    ptrs = [s.data_ptr() for s in src]
+    Q.pack_fermions(bufs[0].data_ptr(), nrm(0), ptrs, Q.QCU_SRC_LEX, 1, prec)  # odd input
+    Q.pack_fermions(bufs[1].data_ptr(), nrm(1), ptrs, Q.QCU_SRC_LEX, 0, prec)  # even x
+    a, b = -0.0144, 1.0
+    Q.dslash_xpay_mrhs(bufs[2].data_ptr(), nrm(2), bufs[0].data_ptr(), nrm(0), bufs[1].data_ptr(), nrm(1), nrhs, 0, 0,
+                       prec, a, b)
+    outs = [torch.zeros((S.half_volume(L), 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
+    Q.unpack_fermions([o.data_ptr() for o in outs], bufs[2].data_ptr(), nrm(2), Q.QCU_SRC_EO_HALF, 0, prec)
+    Q.synchronize()
+    got = np.stack([o.cpu().numpy() for o in outs])
+    want = a * O.dslash(full[:, 1], g, L, 0, 0, True) + b * full[:, 0]
+    assert rel(got, want) < TOL[prec]
+
+
+def test_layout_lex_eo_and_lex_gauge(cuda, qcu_lib):
+    torch, Q = cuda, qcu_lib
+    L = (4, 2, 6, 4)
+    n = 3
+    g = S.random_gauge(L, n, seed=110)
+    psi = S.random_fermions(L, n, 2, seed=111)
+    # gauge given lexicographically: [4][V][N][N]
+    V = 2 * S.half_volume(L)
+    glex = np.stack([O.eo_to_lex(g[mu], L) for mu in range(4)])
+    Q.initGridSize(L, n)
+    dgl = dev(torch, glex)
+    Q.load_gauge_lex(dgl.data_ptr())
+    Q.getDslash(0, 0.0, n, 2, 2)
+    ins = [dev(torch, psi[r]) for r in range(2)]
+    outs = [torch.zeros_like(x) for x in ins]
+    for r in range(2):
+        Q.pushBackFermions(outs[r].data_ptr(), ins[r].data_ptr())
+    Q.startDslash(0, 0)
+    got = np.stack([o.cpu().numpy() for o in outs])
+    assert rel(got, O.dslash(psi, g, L, 0, 0)) < 1e-13
+    # fermion lex <-> eo
+    rng = np.random.default_rng(112)
+    lex = rng.standard_normal((V, 4, n)) + 1j * rng.standard_normal((V, 4, n))
+    dl = dev(torch, lex)
+    de = torch.zeros((2, V // 2, 4, n), dtype=torch.complex128, device="cuda")
+    Q.lex_to_eo(de.data_ptr(), dl.data_ptr(), 4 * n)
+    assert np.array_equal(de.cpu().numpy(), O.lex_to_eo(lex, L))
+    dl2 = torch.zeros_like(dl)
+    Q.eo_to_lex(dl2.data_ptr(), de.data_ptr(), 4 * n)
+    assert np.array_equal(dl2.cpu().numpy(), lex)
+
+
+def test_deprecated_entry_points(cuda, qcu_lib):
+    """dslashQcu / fullDslashQcu (no-op stubs in the reference) compute the hop."""
+    torch, Q = cuda, qcu_lib
+    L = (4, 4, 4, 4)
+    g = S.random_gauge(L, 3, seed=120)
+    full = S.random_fermions(L, 3, 1, seed=121, parities=2)[0]
+    Q.set_antiperiodic_t(False)
+    dg, din = dev(torch, g), dev(torch, full)
+    dout = torch.zeros_like(din)
+    Q.fullDslashQcu(dout.data_ptr(), din.data_ptr(), dg.data_ptr(), L, 1)
+    got = dout.cpu().numpy()
+    for p in (0, 1):
+        assert rel(got[p], O.dslash(full[1 - p][None], g, L, p, 1)[0]) < 1e-13
+    half_in = dev(torch, full[1])
+    half_out = torch.zeros_like(half_in)
+    Q.dslashQcu(half_out.data_ptr(), half_in.data_ptr(), dg.data_ptr(), L, 0)
+    assert rel(half_out.cpu().numpy(), O.dslash(full[1][None], g, L, 0, 0)[0]) < 1e-13
+
+
+def test_cxx_storage_api(cuda, qcu_lib):
+    """qcu::storage::shiftVectorStorage / shiftGaugeStorage (reference C++ API)."""
+    torch, Q = cuda, qcu_lib
+    lib = Q.lib()
+    L = (4, 4, 4, 8)
+    vh = S.half_volume(L)
+    psi = S.random_fermions(L, 3, 1, seed=130)[0]
+    g = S.random_gauge(L, 3, seed=131)
+    fv = getattr(lib, Q.CXX_SYMBOLS[0])
+    fg = getattr(lib, Q.CXX_SYMBOLS[1])
+    for f in (fv, fg):
+        f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_int] * 4
+        f.restype = None
+    src = dev(torch, psi)
+    dst = torch.zeros((12, vh), dtype=torch.complex128, device="cuda")
+    fv(dst.data_ptr(), src.data_ptr(), 0, L[0] // 2, L[1], L[2], L[3])
+    assert np.array_equal(dst.cpu().numpy(), psi.reshape(vh, 12).T)
+    back = torch.zeros_like(src)
+    fv(back.data_ptr(), dst.data_ptr(), 1, L[0] // 2, L[1], L[2], L[3])
+    assert np.array_equal(back.cpu().numpy(), psi)
+    gs = dev(torch, g)
+    gd = torch.zeros((4, 2, 9, vh), dtype=torch.complex128, device="cuda")
+    fg(gd.data_ptr(), gs.data_ptr(), 0, *L)
+    assert np.array_equal(gd.cpu().numpy(), g.reshape(4, 2, vh, 9).transpose(0, 1, 3, 2))
+
+
+def test_full_size_fp32_against_oracle(cuda, qcu_lib):
+    """32^3 x 64, SU(3), nrhs = 12 in FP32 (the benchmark workload): two RHS
+    checked against the oracle, all twelve by linearity across RHS."""
+    torch, Q = cuda, qcu_lib
+    L = (32, 32, 32, 64)
+    g = S.random_gauge(L, 3, seed=140)
+    rng = np.random.default_rng(141)
+    vh = S.half_volume(L)
+    base = (rng.standard_normal((2, vh, 4, 3)) + 1j * rng.standard_normal((2, vh, 4, 3))) * np.sqrt(0.5)
+    coef = rng.standard_normal((12, 2))
+    psi = np.einsum("rk,kvsa->rvsa", coef, base)  # every RHS a combination of the two bases
+    got = abi_dslash(torch, Q, psi, g, L, 1, 0, 1, antiperiodic_t=True)
+    ref = O.dslash(base, g, L, 1, 0, True)
+    want = np.einsum("rk,kvsa->rvsa", coef, ref)
+    for r in range(12):
+        assert rel(got[r], want[r]) < 1e-6
