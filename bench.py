@@ -1,0 +1,465 @@
+#!/usr/bin/env python3
+"""Benchmark of the MRHS even-odd Wilson dslash on GB300.
+
+Workload (one "step"): the hopping term D_eo applied to nrhs = 12 right-hand
+sides of SU(3) spinors on a 32^3 x 64 lattice (Vh = 1,048,576 output sites),
+FP32 storage and arithmetic, antiperiodic time boundaries, seeded random
+SU(3) links and Gaussian spinors (synthetic data; the reference publishes no
+dataset).  The input field (1.2 GB) and gauge (0.6 GB) exceed the 129 MB L2,
+so no flush is needed between steps.
+
+Reported (one JSON line on rank 0):
+  value      site*RHS/s of the device-resident dslash (CUDA events on the
+             library stream around exactly --steps launches)
+  e2e        the same metric through the drop-in C ABI (pushBackFermions x 12 +
+             startDslash) with pinned host buffers: host->device copy of the
+             caller-layout FP64 inputs and device->host copy of the outputs
+             inside the timed region
+  roofline   algorithmic bytes per launch / mean launch time vs measured HBM
+  cpu_baseline  the FP64 OpenMP oracle dslash on this host's cores
+  sweep      site*RHS/s and roofline fraction per precision x nrhs
+  solve      eo-CG to FP64 true residual 1e-10: mixed precision vs plain FP64
+
+--impl reference times the reference's CPU path for this operator on the
+host cores.  The reference has no CPU implementation (its only code path is
+the sm_70-era GPU kernel), so this arm runs the FP64 OpenMP restatement of its
+operator (oracle/), on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_BENCH = (32, 32, 32, 64)
+NRHS = 12
+NC = 3
+FLOPS_PER_SITE_RHS = lambda n: 128 * n * n + 56 * n  # noqa: E731
+
+
+def bytes_per_site_rhs(prec: int, n: int, nrhs: int) -> float:
+    """Compulsory bytes per output site per RHS: 8 links (N^2 complex each,
+    amortised over the RHS) + one input and one output spinor (4N complex)
+    + the per-(site, RHS) FP32 scale of 16-bit storage, read and written."""
+    c = {2: 16, 1: 8, 0: 4, 4: 4}[prec]
+    nn = 4 if prec in (0, 4) else 0
+    return 8 * n * n * c / nrhs + 2 * (4 * n * c + nn)
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the headline kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dslash_traffic.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    """One process per GPU under torchrun; replicas of the workload (the RHS
+    sets are independent, so no data-path collective exists)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1):
+    """Seeded SU(N) gauge and Gaussian spinors, generated on the GPU with the
+    phase-fixed QR construction (QR -> phases of diag(R) into Q -> det^(-1/N))."""
+    from mrhs_qcu_gb300 import synthetic as S
+    vh = S.half_volume(L)
+    gen = torch.Generator(device="cuda").manual_seed(seed_g)
+    g = torch.empty((4, 2, vh, n, n), dtype=torch.complex128, device="cuda")
+    flat = g.view(-1, n, n)
+    chunk = 1 << 20
+    for s in range(0, flat.shape[0], chunk):
+        m = min(chunk, flat.shape[0] - s)
+        a = torch.complex(torch.randn((m, n, n), generator=gen, device="cuda", dtype=torch.float64),
+                          torch.randn((m, n, n), generator=gen, device="cuda", dtype=torch.float64)) * (0.5 ** 0.5)
+        q, r = torch.linalg.qr(a)
+        d = torch.diagonal(r, dim1=-2, dim2=-1)
+        q = q * (d / d.abs()).unsqueeze(-2)
+        det = torch.linalg.det(q)
+        q = q * (det ** (-1.0 / n)).view(-1, 1, 1)
+        flat[s:s + m] = q
+    genp = torch.Generator(device="cuda").manual_seed(seed_p)
+    psi = torch.complex(torch.randn((nrhs, vh, 4, n), generator=genp, device="cuda", dtype=torch.float64),
+                        torch.randn((nrhs, vh, 4, n), generator=genp, device="cuda", dtype=torch.float64)) * (0.5 ** 0.5)
+    return g, psi
+
+
+def time_resident(torch, Q, L, n, nrhs, prec, steps, warmup, g_dev, psi_dev, count_launches=True):
+    """Device-resident dslash: pack once, then time `steps` MRHS launches."""
+    from mrhs_qcu_gb300 import synthetic as S
+    vh = S.half_volume(L)
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    Q.set_stream(torch.cuda.current_stream().cuda_stream)
+    Q.loadQcuGauge(g_dev.data_ptr())
+    Q.getDslash(Q.DSLASH_WILSON, 0.0, n, nrhs, prec)
+    db, nb = Q.field_bytes(prec, nrhs)
+    fin = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
+    fout = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
+    nin = torch.empty(max(nb, 16) // 4, dtype=torch.float32, device="cuda") if nb else None
+    nout = torch.empty(max(nb, 16) // 4, dtype=torch.float32, device="cuda") if nb else None
+    ptrs = [psi_dev[r % psi_dev.shape[0]].data_ptr() for r in range(nrhs)]
+    Q.pack_fermions(fin.data_ptr(), nin.data_ptr() if nin is not None else None, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
+    args = (fout.data_ptr(), nout.data_ptr() if nout is not None else None, fin.data_ptr(),
+            nin.data_ptr() if nin is not None else None, nrhs, 0, 0, prec)
+    Q.tune_dslash(nrhs, prec)
+    for _ in range(max(warmup, 1)):
+        Q.dslash_mrhs(*args)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        Q.dslash_mrhs(*args)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    Q.set_stream(None)
+    return ms, vh * nrhs
+
+
+def run_gpu(args):
+    import torch
+
+    import mrhs_qcu_gb300 as Q
+    from mrhs_qcu_gb300 import synthetic as S
+
+    world, rank, local, dist = dist_setup()
+    torch.cuda.set_device(local)
+    L, n, nrhs, prec = L_BENCH, NC, NRHS, Q.QCU_SINGLE_PRECISION
+    vh = S.half_volume(L)
+    g_dev, psi_dev = make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1 + rank)
+
+    # ---- device-resident headline --------------------------------------
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    stream = torch.cuda.current_stream()
+    Q.set_stream(stream.cuda_stream)
+    Q.loadQcuGauge(g_dev.data_ptr())
+    Q.getDslash(Q.DSLASH_WILSON, 0.0, n, nrhs, prec)
+    db, _ = Q.field_bytes(prec, nrhs)
+    fin = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
+    fout = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
+    ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
+    Q.pack_fermions(fin.data_ptr(), None, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
+    R, block = Q.tune_dslash(nrhs, prec)
+    for _ in range(args.warmup):
+        Q.dslash_mrhs(fout.data_ptr(), None, fin.data_ptr(), None, nrhs, 0, 0, prec)
+    torch.cuda.synchronize()
+    barrier(dist)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            Q.dslash_mrhs(fout.data_ptr(), None, fin.data_ptr(), None, nrhs, 0, 0, prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(dist)
+    ms_local = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(dist, ms_local)
+    units = vh * nrhs
+    value = units * world / (ms * 1e-3)
+    peak, peak_kind = measured_peaks()
+    bpu = bytes_per_site_rhs(prec, n, nrhs)
+    achieved = bpu * units / (ms_local * 1e-3) / 1e9
+    traffic = profile_traffic()
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bpu * units,
+            "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+            "kernel": "wilson_mrhs_kernel<fp32,N=3,R=%d> block %d" % (R, block),
+            "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
+    Q.set_stream(None)
+
+    # ---- end to end through the drop-in ABI with host buffers -----------
+    e2e = None
+    if not args.skip_e2e:
+        host_in = [torch.empty((vh, 4, n), dtype=torch.complex128).pin_memory() for _ in range(nrhs)]
+        for r in range(nrhs):
+            host_in[r].copy_(psi_dev[r])
+        host_out = [torch.empty((vh, 4, n), dtype=torch.complex128).pin_memory() for _ in range(nrhs)]
+        dev_in = [torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
+        dev_out = [torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
+        Q.set_stream(stream.cuda_stream)
+
+        def e2e_step():
+            for r in range(nrhs):
+                dev_in[r].copy_(host_in[r], non_blocking=True)
+            for r in range(nrhs):
+                Q.pushBackFermions(dev_out[r].data_ptr(), dev_in[r].data_ptr())
+            Q.startDslash(0, 0)
+            for r in range(nrhs):
+                host_out[r].copy_(dev_out[r], non_blocking=True)
+
+        for _ in range(max(1, args.warmup // 2)):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_steps = max(1, min(args.steps, 5))
+        barrier(dist)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ems = max_over_ranks(dist, f0.elapsed_time(f1) / e2e_steps)
+        bytes_io = nrhs * vh * 4 * n * 16
+        e2e = {"value": units * world / (ems * 1e-3), "unit": "site*RHS/s", "h2d_bytes_per_step": bytes_io,
+               "d2h_bytes_per_step": bytes_io, "ms_per_step": round(ems, 3), "steps": e2e_steps,
+               "path": "pinned host -> pushBackFermions x12 -> startDslash -> pinned host (FP64 caller layout)"}
+        Q.set_stream(None)
+        del host_in, host_out, dev_in, dev_out
+
+    del fin, fout
+    torch.cuda.empty_cache()
+
+    # ---- sweep of precisions x nrhs ------------------------------------
+    sweep = []
+    if not args.skip_sweep and rank == 0:
+        for p, pname in ((2, "fp64"), (1, "fp32"), (0, "fp16"), (4, "bf16")):
+            for nr in (1, 4, 12, 24):
+                if p == 2 and nr == 24:
+                    continue
+                ms_s, u = time_resident(torch, Q, L, n, nr, p, 5 if p != 2 else 2, 2, g_dev, psi_dev)
+                ach = bytes_per_site_rhs(p, n, nr) * u / (ms_s * 1e-3) / 1e9
+                sweep.append({"precision": pname, "nrhs": nr, "ms": round(ms_s, 4),
+                              "site_rhs_per_s": round(u / (ms_s * 1e-3)),
+                              "gbs": round(ach, 1), "hbm_frac": round(ach / peak, 4),
+                              "gflops": round(FLOPS_PER_SITE_RHS(n) * u / (ms_s * 1e-3) / 1e9, 1)})
+        torch.cuda.empty_cache()
+
+    # ---- CPU baseline (oracle, FP64, host cores) -----------------------
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu = cpu_baseline(g_dev, psi_dev, L, n, budget_s=args.cpu_seconds)
+
+    # ---- solver: mixed vs FP64 ----------------------------------------
+    solve = None
+    if rank == 0 and not args.skip_solve:
+        solve = solve_bench(torch, Q)
+
+    if rank == 0:
+        line = {
+            "metric": "dslash site*RHS/s (SU(3) 32^3x64, nrhs=12, FP32) & % HBM roofline",
+            "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (complex fp32)", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
+            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), 32^3x64, nrhs=12, FP32, "
+                                   "antiperiodic t", "lattice": list(L), "nrhs": nrhs, "N": n,
+                       "precision": "fp32", "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
+                       "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
+            "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
+            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "solve": solve,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(g_dev, psi_dev, L, n, budget_s=12.0):
+    """FP64 OpenMP oracle dslash on the host cores, on a bounded sample of the
+    workload: the full 32^3x64 gauge, as many RHS of the benchmark field as fit
+    the time budget (one RHS per call)."""
+    from oracle import oracle as O
+    g = g_dev.cpu().numpy()
+    threads = O.num_threads()
+    from mrhs_qcu_gb300 import synthetic as S
+    vh = S.half_volume(L)
+    done = 0
+    t0 = time.perf_counter()
+    elapsed = 0.0
+    r = 0
+    while elapsed < budget_s and r < psi_dev.shape[0]:
+        psi = psi_dev[r:r + 1].cpu().numpy()
+        t1 = time.perf_counter()
+        O.dslash(psi, g, L, 0, 0, True)
+        elapsed += time.perf_counter() - t1
+        done += vh
+        r += 1
+    return {"value": done / elapsed, "unit": "site*RHS/s", "cores": threads, "kind": "port",
+            "sample": "%d RHS of the 32^3x64 SU(3) field, FP64, %.1f s" % (r, elapsed),
+            "wall_s": round(time.perf_counter() - t0, 2)}
+
+
+def solve_bench(torch, Q):
+    """eo-CG on Mhat^dag Mhat to FP64 true residual 1e-10, 24^3x48, SU(3),
+    nrhs=12, kappa=0.12, point sources: FP32 / FP16 inner with FP64 reliable
+    updates vs the plain FP64 MRHS CG."""
+    from mrhs_qcu_gb300 import synthetic as S
+    L, n, nrhs, kappa = (24, 24, 24, 48), 3, 12, 0.12
+    g_dev, _ = make_inputs(torch, L, n, 1, seed_g=5)
+    b = S.point_sources(L, n, nrhs, seed=6)
+    db = [torch.from_numpy(b[r]).cuda() for r in range(nrhs)]
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    Q.loadQcuGauge(g_dev.data_ptr())
+    out = {"workload": "24^3x48 SU(3) nrhs=12 kappa=0.12 point sources, tol 1e-10 (FP64 true residual)"}
+    for name, inner in (("fp32_inner", 1), ("fp16_inner", 0), ("fp64_plain", 2)):
+        dx = [torch.zeros_like(x) for x in db]
+        p = Q.solver_params(kappa=kappa, tol=1e-10, inner_precision=inner, max_iter=20000)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Q.invert([x.data_ptr() for x in dx], [x.data_ptr() for x in db], p, raise_on_error=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[name] = {"seconds": round(dt, 3), "iterations": p.iterations, "reliable_updates": p.reliable_updates,
+                     "max_true_residual": max(p.true_residual[r] for r in range(nrhs)),
+                     "all_converged": all(p.converged[r] for r in range(nrhs))}
+    if out["fp64_plain"]["seconds"] > 0:
+        out["speedup_fp32_inner_vs_fp64"] = round(out["fp64_plain"]["seconds"] / out["fp32_inner"]["seconds"], 2)
+        out["speedup_fp16_inner_vs_fp64"] = round(out["fp64_plain"]["seconds"] / out["fp16_inner"]["seconds"], 2)
+    return out
+
+
+def run_reference(args):
+    """The reference's CPU path for this operator: FP64 OpenMP restatement
+    (the reference itself has no CPU implementation), all host threads."""
+    world, rank, local, dist = dist_setup()
+    if rank != 0:
+        return
+    from mrhs_qcu_gb300 import synthetic as S
+    from oracle import oracle as O
+    L, n, nrhs = L_BENCH, NC, NRHS
+    g = S.random_gauge(L, n, seed=0)
+    vh = S.half_volume(L)
+    rng = np.random.default_rng(1)
+    psi = (rng.standard_normal((1, vh, 4, n)) + 1j * rng.standard_normal((1, vh, 4, n))) * np.sqrt(0.5)
+    for _ in range(args.warmup):
+        O.dslash(psi, g, L, 0, 0, True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.dslash(psi, g, L, 0, 0, True)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = vh / dt
+    line = {"impl": "reference", "metric": "dslash site*RHS/s (SU(3) 32^3x64, nrhs=12, FP32) & % HBM roofline",
+            "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128 (complex fp64)", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
+            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), 32^3x64, nrhs=12, antiperiodic t",
+                       "lattice": list(L), "nrhs": nrhs, "N": n},
+            "cpu_baseline": {"value": value, "unit": "site*RHS/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": "one RHS of the 32^3x64 SU(3) workload per step (1/12 of a step), FP64"},
+            "e2e": {"value": value, "unit": "site*RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-sweep", action="store_true")
+    ap.add_argument("--skip-solve", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -30,6 +30,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "session.h"
@@ -463,6 +465,12 @@ class Solver {
       act[r] = converged_[r] ? 0 : 1;
       any |= act[r] != 0;
     }
+    if (verbose_) {
+      fprintf(stderr, "qcu solver: reliable update %d, true |s|/|b| per RHS:", updates_);
+      for (int r = 0; r < n_; r++) fprintf(stderr, " %.3e", std::sqrt(ss_true_host_[r] / bb_host_[r]));
+      fprintf(stderr, "\n");
+    }
+    updates_++;
     QCU_CHECK_CUDA(cudaMemcpyAsync(S_.active, act.data(), sizeof(int) * n_, cudaMemcpyHostToDevice, st_));
     QCU_CHECK_CUDA(cudaMemcpyAsync(S_.maxss, S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st_));
     QCU_CHECK_CUDA(cudaMemcpyAsync(S_.ss, S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st_));
@@ -491,6 +499,8 @@ class Solver {
   std::vector<int> converged_;
   cudaGraphExec_t graph_exec_ = nullptr;
   bool warm_ = false;
+  bool verbose_ = getenv("QCU_SOLVER_VERBOSE") != nullptr;
+  int updates_ = 0;
 };
 
 }  // namespace

@@ -142,6 +142,7 @@ def test_layout_lex_eo_and_lex_gauge(cuda, qcu_lib):
     V = 2 * S.half_volume(L)
     glex = np.stack([O.eo_to_lex(g[mu], L) for mu in range(4)])
     Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(False)
     dgl = dev(torch, glex)
     Q.load_gauge_lex(dgl.data_ptr())
     Q.getDslash(0, 0.0, n, 2, 2)
