@@ -221,7 +221,9 @@ def run_gpu(args):
 
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
-    L, n, nrhs, prec = L_BENCH, NC, NRHS, Q.QCU_SINGLE_PRECISION
+    L = tuple(int(v) for v in args.lattice.split(","))
+    n, nrhs, prec = NC, args.nrhs, args.precision
+    pname = {0: "fp16", 1: "fp32", 2: "fp64", 4: "bf16"}[prec]
     vh = S.half_volume(L)
     g_dev, psi_dev = make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1 + rank)
 
@@ -232,14 +234,18 @@ def run_gpu(args):
     Q.set_stream(stream.cuda_stream)
     Q.loadQcuGauge(g_dev.data_ptr())
     Q.getDslash(Q.DSLASH_WILSON, 0.0, n, nrhs, prec)
-    db, _ = Q.field_bytes(prec, nrhs)
+    db, nb = Q.field_bytes(prec, nrhs)
     fin = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
     fout = torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda")
+    nin = torch.empty(max(nb, 16) // 4, dtype=torch.float32, device="cuda") if nb else None
+    nout = torch.empty(max(nb, 16) // 4, dtype=torch.float32, device="cuda") if nb else None
+    nin_p = nin.data_ptr() if nin is not None else None
+    nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
-    Q.pack_fermions(fin.data_ptr(), None, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
+    Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
     R, block = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
-        Q.dslash_mrhs(fout.data_ptr(), None, fin.data_ptr(), None, nrhs, 0, 0, prec)
+        Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
     barrier(dist)
     e0 = torch.cuda.Event(enable_timing=True)
@@ -248,7 +254,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(args.steps):
-            Q.dslash_mrhs(fout.data_ptr(), None, fin.data_ptr(), None, nrhs, 0, 0, prec)
+            Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
         e1.record(stream)
         torch.cuda.synchronize()
     barrier(dist)
@@ -264,7 +270,7 @@ def run_gpu(args):
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
             "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
-            "kernel": "wilson_mrhs_kernel<fp32,N=3,R=%d> block %d" % (R, block),
+            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d> block %d" % (pname, R, block),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 
@@ -342,9 +348,9 @@ def run_gpu(args):
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c64 (complex fp32)", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
-            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), 32^3x64, nrhs=12, FP32, "
-                                   "antiperiodic t", "lattice": list(L), "nrhs": nrhs, "N": n,
-                       "precision": "fp32", "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
+            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), %s, nrhs=%d, %s, antiperiodic t"
+                                   % ("x".join(map(str, L)), nrhs, pname.upper()), "lattice": list(L), "nrhs": nrhs,
+                       "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
             "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
             "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "solve": solve,
@@ -452,7 +458,14 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--lattice", default="32,32,32,64", help="X,Y,Z,T of the headline workload")
+    ap.add_argument("--nrhs", type=int, default=NRHS)
+    ap.add_argument("--precision", type=int, default=1, help="0 fp16, 1 fp32, 2 fp64, 4 bf16")
+    ap.add_argument("--profile", action="store_true",
+                    help="headline kernel only (no e2e, sweep, CPU or solve legs), for ncu captures")
     args = ap.parse_args()
+    if args.profile:
+        args.skip_sweep = args.skip_solve = args.skip_cpu = args.skip_e2e = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -73,6 +73,15 @@ void Autotuner::save_file() {
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
+  // QCU_DSLASH_CONFIG="R,block" pins the kernel shape (profiling, sweeps)
+  if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
+    DslashConfig c;
+    if (sscanf(f, "%d,%d", &c.R, &c.block) == 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R) &&
+        c.block >= 32 && c.block <= 1024 && c.block % 32 == 0) {
+      *found = true;
+      return c;
+    }
+  }
   if (!file_loaded_) load_file();
   auto it = cache_.find(key(prec, N, nrhs, vh));
   *found = it != cache_.end();

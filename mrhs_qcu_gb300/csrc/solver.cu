@@ -108,6 +108,19 @@ __global__ void cg_beta_kernel(Scalars S, int nrhs, double delta2) {
   }
 }
 
+// After a reliable update replaces r by the recomputed residual, restore the
+// CG invariant <r, p> = |r|^2 by p <- p + c r, c = 1 - <r, p> / |r|^2 (tmp1 =
+// <r, p>).  With a 16-bit operator the iterated residual drifts away from the
+// true one between updates; keeping p unchanged then breaks conjugacy.
+__global__ void cg_restore_kernel(Scalars S, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs) return;
+  double2 c = make_double2(0.0, 0.0);
+  const double rr = S.rr[r];
+  if (S.active[r] && rr > 0.0 && isfinite(rr)) c = make_double2(1.0 - S.tmp1[r].x / rr, -S.tmp1[r].y / rr);
+  S.tmp2[r] = c;
+}
+
 // BiCGStab: alpha = rho / <r0, v>
 __global__ void bicg_alpha_kernel(Scalars S, int nrhs) {
   const int r = threadIdx.x;
@@ -315,12 +328,13 @@ class Solver {
       B.cdot(ref(r0l_, s_), ref(sl_, s_), S_.rho, st_);
     }
     while (any_active && iters < q_.max_iter) {
-      const int k = std::min(kChunk, q_.max_iter - iters);
+      const int k = std::min(chunk_, q_.max_iter - iters);
       run_chunk(k);
       iters += k;
       int status[3];
       QCU_CHECK_CUDA(cudaMemcpyAsync(status, S_.status, sizeof(int) * 3, cudaMemcpyDeviceToHost, st_));
       QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+      if (verbose_) trace(iters, status);
       if (status[1] || status[0] == 0 || status[2]) {
         any_active = reliable_update(false);
         res.reliable_updates++;
@@ -415,7 +429,7 @@ class Solver {
 
   void run_chunk(int k) {
     QCU_CHECK_CUDA(cudaMemsetAsync(S_.status, 0, sizeof(int) * 3, st_));
-    if (q_.use_graph && k == kChunk) {
+    if (q_.use_graph && k == chunk_) {
       if (!graph_exec_) {
         // the kernel shapes must be tuned before capture; one eager chunk does it
         if (!warm_) {
@@ -479,6 +493,11 @@ class Solver {
     if (q_.solver == 0) {
       op_apply(rl_, sl_, 1);  // r = Mhat^dag s
       B.norm2(ref(rl_, s_), S_.rr, st_);
+      if (!first) {
+        B.cdot(ref(rl_, s_), ref(pl_, s_), S_.tmp1, st_);
+        cg_restore_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+        B.axpby(S_.tmp2, ref(rl_, s_), nullptr, ref(pl_, s_), st_);  // p += c r
+      }
     }
     QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
     return any;
@@ -501,6 +520,21 @@ class Solver {
   bool warm_ = false;
   bool verbose_ = getenv("QCU_SOLVER_VERBOSE") != nullptr;
   int updates_ = 0;
+  int chunk_ = getenv("QCU_SOLVER_CHUNK") ? std::max(1, atoi(getenv("QCU_SOLVER_CHUNK"))) : kChunk;
+
+  // per-chunk scalars of RHS 0 (QCU_SOLVER_VERBOSE)
+  void trace(int iters, const int* status) {
+    double v[5];
+    double2 c[2];
+    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[0], S_.rr, sizeof(double), cudaMemcpyDeviceToHost, st_));
+    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[1], S_.qq, sizeof(double), cudaMemcpyDeviceToHost, st_));
+    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[2], S_.ss, sizeof(double), cudaMemcpyDeviceToHost, st_));
+    QCU_CHECK_CUDA(cudaMemcpyAsync(&c[0], S_.alpha, sizeof(double2), cudaMemcpyDeviceToHost, st_));
+    QCU_CHECK_CUDA(cudaMemcpyAsync(&c[1], S_.beta, sizeof(double2), cudaMemcpyDeviceToHost, st_));
+    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+    fprintf(stderr, "qcu solver: iter %d active %d update %d | rhs0 rr %.3e qq %.3e ss/bb %.3e alpha %.3e beta %.3e\n",
+            iters, status[0], status[1], v[0], v[1], v[2] / bb_host_[0], c[0].x, c[1].x);
+  }
 };
 
 }  // namespace
