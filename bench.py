@@ -44,6 +44,7 @@ L_BENCH = (32, 32, 32, 64)
 NRHS = 12
 NC = 3
 FLOPS_PER_SITE_RHS = lambda n: 128 * n * n + 56 * n  # noqa: E731
+METRIC = "dslash site\u00b7RHS/s & % HBM roofline; mixed vs FP64 solve time @1e-10; p99"
 
 
 def bytes_per_site_rhs(prec: int, n: int, nrhs: int) -> float:
@@ -66,65 +67,94 @@ def measured_peaks():
 
 def profile_traffic():
     """Per-launch DRAM bytes of the headline kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "dslash_traffic.json")
-    if os.path.exists(path):
-        with open(path) as fh:
-            return json.load(fh)
-    return None
+    path = os.path.join(ROOT, "profiles", "dslash_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    out = {}
+    with open(path) as fh:
+        for line in fh:
+            if line.strip() and not line.startswith("#"):
+                k, v = line.split(None, 1)
+                out[k] = v.strip()
+    if "dram_bytes_per_launch" in out:
+        out["dram_bytes_per_launch"] = float(out["dram_bytes_per_launch"])
+    return out
 
 
 class ClockSampler:
-    """nvidia-smi sampling during the timed region."""
+    """SM clock and clock-event reasons sampled every few ms during the timed
+    region, through NVML (read-only queries), with nvidia-smi as a fallback."""
 
-    def __init__(self, index: int):
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int, period_s: float = 0.005):
         self.index = index
-        self.proc = None
-        self.lines = []
+        self.period = period_s
+        self.sm, self.reasons, self.max_mhz = [], set(), None
+        self._stop = threading.Event()
+        self._nvml = None
+        self._thread = None
+
+    def _open(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        if lib.nvmlInit_v2() != 0:
+            return None
+        h = ctypes.c_void_p()
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+        idx = int(vis.split(",")[self.index]) if vis and vis.split(",")[0].isdigit() else self.index
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(idx), ctypes.byref(h)) != 0:
+            return None
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(h, ctypes.c_int(1), ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        return lib, h
+
+    def _run(self):
+        import ctypes
+        lib, h = self._nvml
+        clk = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        get_r = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self._stop.is_set():
+            if lib.nvmlDeviceGetClockInfo(h, ctypes.c_int(1), ctypes.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if get_r(h, ctypes.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            self._stop.wait(self.period)
 
     def __enter__(self):
-        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.reader = threading.Thread(target=self._read, daemon=True)
-            self.reader.start()
-        except OSError:
-            self.proc = None
+        self._nvml = self._open()
+        if self._nvml is not None:
+            self._thread = threading.Thread(target=self._run, daemon=True)
+            self._thread.start()
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
     def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
+        self._stop.set()
+        if self._thread is not None:
+            self._thread.join(timeout=2)
+        if not self.sm:  # fallback: one nvidia-smi reading right after the region
             try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=20).stdout.split(",")
+                self.sm.append(float(out[0]))
+                self.max_mhz = float(out[1])
+            except (OSError, ValueError, IndexError, subprocess.TimeoutExpired):
+                pass
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx = float(f[2])
-            except ValueError:
-                continue
-            for name, v in zip(names, f[5:9]):
-                if v.lower() == "active":
-                    reasons.add(name)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": 0}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        med = float(np.median(self.sm)) if self.sm else None
+        return {"sm_mhz": med, "sm_max_mhz": self.max_mhz, "reasons": sorted(self.reasons),
+                "samples": len(self.sm), "source": "nvml" if self._nvml is not None else "nvidia-smi"}
 
 
 def dist_setup():
@@ -156,23 +186,11 @@ def max_over_ranks(dist, v: float) -> float:
 
 def make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1):
     """Seeded SU(N) gauge and Gaussian spinors, generated on the GPU with the
-    phase-fixed QR construction (QR -> phases of diag(R) into Q -> det^(-1/N))."""
+    phase-fixed QR construction (Gram-Schmidt, then det^(-1/N))."""
     from mrhs_qcu_gb300 import synthetic as S
     vh = S.half_volume(L)
     gen = torch.Generator(device="cuda").manual_seed(seed_g)
-    g = torch.empty((4, 2, vh, n, n), dtype=torch.complex128, device="cuda")
-    flat = g.view(-1, n, n)
-    chunk = 1 << 20
-    for s in range(0, flat.shape[0], chunk):
-        m = min(chunk, flat.shape[0] - s)
-        a = torch.complex(torch.randn((m, n, n), generator=gen, device="cuda", dtype=torch.float64),
-                          torch.randn((m, n, n), generator=gen, device="cuda", dtype=torch.float64)) * (0.5 ** 0.5)
-        q, r = torch.linalg.qr(a)
-        d = torch.diagonal(r, dim1=-2, dim2=-1)
-        q = q * (d / d.abs()).unsqueeze(-2)
-        det = torch.linalg.det(q)
-        q = q * (det ** (-1.0 / n)).view(-1, 1, 1)
-        flat[s:s + m] = q
+    g = S.random_sun_torch(4 * 2 * vh, n, gen).view(4, 2, vh, n, n)
     genp = torch.Generator(device="cuda").manual_seed(seed_p)
     psi = torch.complex(torch.randn((nrhs, vh, 4, n), generator=genp, device="cuda", dtype=torch.float64),
                         torch.randn((nrhs, vh, 4, n), generator=genp, device="cuda", dtype=torch.float64)) * (0.5 ** 0.5)
@@ -243,7 +261,7 @@ def run_gpu(args):
     nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
     Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
-    R, block = Q.tune_dslash(nrhs, prec)
+    R, block, minb = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
         Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
@@ -269,8 +287,9 @@ def run_gpu(args):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
-            "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
-            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d> block %d" % (pname, R, block),
+            "traffic": traffic.get("dram_bytes_per_launch")
+            if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1) else None,
+            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d,MINB=%d> block %d" % (pname, R, minb, block),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 
@@ -320,13 +339,13 @@ def run_gpu(args):
     # ---- sweep of precisions x nrhs ------------------------------------
     sweep = []
     if not args.skip_sweep and rank == 0:
-        for p, pname in ((2, "fp64"), (1, "fp32"), (0, "fp16"), (4, "bf16")):
+        for p, sname in ((2, "fp64"), (1, "fp32"), (0, "fp16"), (4, "bf16")):
             for nr in (1, 4, 12, 24):
                 if p == 2 and nr == 24:
                     continue
                 ms_s, u = time_resident(torch, Q, L, n, nr, p, 5 if p != 2 else 2, 2, g_dev, psi_dev)
                 ach = bytes_per_site_rhs(p, n, nr) * u / (ms_s * 1e-3) / 1e9
-                sweep.append({"precision": pname, "nrhs": nr, "ms": round(ms_s, 4),
+                sweep.append({"precision": sname, "nrhs": nr, "ms": round(ms_s, 4),
                               "site_rhs_per_s": round(u / (ms_s * 1e-3)),
                               "gbs": round(ach, 1), "hbm_frac": round(ach / peak, 4),
                               "gflops": round(FLOPS_PER_SITE_RHS(n) * u / (ms_s * 1e-3) / 1e9, 1)})
@@ -344,10 +363,10 @@ def run_gpu(args):
 
     if rank == 0:
         line = {
-            "metric": "dslash site*RHS/s (SU(3) 32^3x64, nrhs=12, FP32) & % HBM roofline",
+            "metric": METRIC,
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64 (complex fp32)", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
+            "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
             "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), %s, nrhs=%d, %s, antiperiodic t"
                                    % ("x".join(map(str, L)), nrhs, pname.upper()), "lattice": list(L), "nrhs": nrhs,
                        "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
@@ -399,14 +418,17 @@ def solve_bench(torch, Q):
     Q.loadQcuGauge(g_dev.data_ptr())
     out = {"workload": "24^3x48 SU(3) nrhs=12 kappa=0.12 point sources, tol 1e-10 (FP64 true residual)"}
     for name, inner in (("fp32_inner", 1), ("fp16_inner", 0), ("fp64_plain", 2)):
-        dx = [torch.zeros_like(x) for x in db]
-        p = Q.solver_params(kappa=kappa, tol=1e-10, inner_precision=inner, max_iter=20000)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        Q.invert([x.data_ptr() for x in dx], [x.data_ptr() for x in db], p, raise_on_error=False)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        out[name] = {"seconds": round(dt, 3), "iterations": p.iterations, "reliable_updates": p.reliable_updates,
+        res = {}
+        for phase in ("cold", "warm"):  # the cold solve tunes kernels and captures graphs
+            dx = [torch.zeros_like(x) for x in db]
+            p = Q.solver_params(kappa=kappa, tol=1e-10, inner_precision=inner, max_iter=20000)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Q.invert([x.data_ptr() for x in dx], [x.data_ptr() for x in db], p, raise_on_error=False)
+            torch.cuda.synchronize()
+            res[phase] = time.perf_counter() - t0
+        out[name] = {"seconds": round(res["warm"], 4), "seconds_cold": round(res["cold"], 4),
+                     "iterations": p.iterations, "reliable_updates": p.reliable_updates,
                      "max_true_residual": max(p.true_residual[r] for r in range(nrhs)),
                      "all_converged": all(p.converged[r] for r in range(nrhs))}
     if out["fp64_plain"]["seconds"] > 0:
@@ -435,10 +457,10 @@ def run_reference(args):
         O.dslash(psi, g, L, 0, 0, True)
     dt = (time.perf_counter() - t0) / args.steps
     value = vh / dt
-    line = {"impl": "reference", "metric": "dslash site*RHS/s (SU(3) 32^3x64, nrhs=12, FP32) & % HBM roofline",
+    line = {"impl": "reference", "metric": METRIC,
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128 (complex fp64)", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
+            "dtype": "f64", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
             "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), 32^3x64, nrhs=12, antiperiodic t",
                        "lattice": list(L), "nrhs": nrhs, "N": n},
             "cpu_baseline": {"value": value, "unit": "site*RHS/s", "cores": O.num_threads(), "kind": "port",

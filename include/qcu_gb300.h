@@ -11,7 +11,8 @@
  * records the error for qcuGetLastError().  Pointers are device pointers.
  *
  * Internal MRHS field of one parity (for the session lattice and N):
- *   data  [Vh][4N][nrhs] complex in the field precision (RHS innermost)
+ *   data  [4N][Vh][nrhs] complex in the field precision (component-major,
+ *         RHS innermost)
  *   norm  [Vh][nrhs] float, present only for 16-bit storage; stored values
  *         are component / norm(site, rhs)
  * Sizes come from qcuFieldBytes.  Buffers must be 16-byte aligned.
@@ -97,8 +98,9 @@ int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_
                       const void *x_norm, int nrhs, int parity, int dagger, int precision, double a, double b);
 
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
- * Returns the chosen RHS-per-thread and block size. */
-int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block);
+ * Returns the chosen RHS-per-thread, block size and register-cap variant
+ * (minimum resident 256-thread blocks per SM). */
+int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *min_blocks);
 
 typedef struct QcuSolverParam_s {
   int solver;          /* QCU_SOLVER_CG or QCU_SOLVER_BICGSTAB */

@@ -14,18 +14,25 @@ std::mutex& registry_mutex() {
   static std::mutex m;
   return m;
 }
-int key(int prec, int N, int R) { return (prec * 16 + N) * 16 + R; }
+int key(int prec, int N, int R, int minb) { return ((prec * 16 + N) * 16 + R) * 8 + minb; }
 }  // namespace
 
-void register_dslash(int prec, int N, int R, DslashLauncher fn) {
+void register_dslash(int prec, int N, int R, int minb, DslashLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[key(prec, N, R)] = fn;
+  registry()[key(prec, N, R, minb)] = fn;
 }
 
-DslashLauncher find_dslash(int prec, int N, int R) {
+DslashLauncher find_dslash(int prec, int N, int R, int minb) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find(key(prec, N, R));
+  auto it = registry().find(key(prec, N, R, minb));
   return it == registry().end() ? nullptr : it->second;
+}
+
+int dslash_minb_options(int prec, int N, int R, int* out, int max) {
+  int n = 0;
+  for (int m = 1; m <= 7 && n < max; m++)
+    if (find_dslash(prec, N, R, m)) out[n++] = m;
+  return n;
 }
 
 int dslash_r_options(int prec, int N, int* out, int max) {
@@ -36,10 +43,12 @@ int dslash_r_options(int prec, int N, int* out, int max) {
 }
 
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st) {
-  DslashLauncher fn = find_dslash(prec, N, cfg.R);
+  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb);
   QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
               std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +
-                  ", R=" + std::to_string(cfg.R));
+                  ", R=" + std::to_string(cfg.R) + ", minb=" + std::to_string(cfg.minb));
+  QCU_REQUIRE(cfg.block >= 32 && cfg.block <= 256 && cfg.block % 32 == 0, QCU_ERR_INVALID_ARGUMENT,
+              "dslash block size must be a multiple of 32 in 32..256");
   QCU_REQUIRE(A.nrhs % cfg.R == 0, QCU_ERR_INVALID_ARGUMENT, "nrhs not a multiple of R");
   QCU_REQUIRE((int64_t)A.geo.vh * (A.nrhs / cfg.R) < (1ll << 31), QCU_ERR_INVALID_ARGUMENT,
               "lattice x nrhs too large for one launch");

@@ -5,10 +5,11 @@ namespace qcu {
 namespace {
 struct Register_d3 {
   Register_d3() {
-    register_dslash(PREC_DOUBLE, 3, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1>);
-    register_dslash(PREC_DOUBLE, 3, 2, &launch_wilson_mrhs<PREC_DOUBLE, 3, 2>);
-    register_dslash(PREC_DOUBLE, 3, 3, &launch_wilson_mrhs<PREC_DOUBLE, 3, 3>);
-    register_dslash(PREC_DOUBLE, 3, 4, &launch_wilson_mrhs<PREC_DOUBLE, 3, 4>);
+    register_dslash(PREC_DOUBLE, 3, 1, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 1>);
+    register_dslash(PREC_DOUBLE, 3, 1, 2, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 2>);
+    register_dslash(PREC_DOUBLE, 3, 2, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 2, 1>);
+    register_dslash(PREC_DOUBLE, 3, 3, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 3, 1>);
+    register_dslash(PREC_DOUBLE, 3, 4, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 4, 1>);
   }
 } register_d3;
 }  // namespace

@@ -169,14 +169,16 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 
   // project: h_u = psi_u + s g(u) psi_perm(u), u = 0, 1
   C2<T> h[2][N][R];
-  const E* base = in + (nb * 4 * N) * nrhs + rhs0;
+  // component-major field: component c of site nb at (c * Vh + nb) * nrhs
+  const int64_t cs = vh * nrhs;
+  const E* base = in + nb * nrhs + rhs0;
 #pragma unroll
   for (int a = 0; a < N; a++) {
     VecBuf<E, R> p0, p1, q0, q1;
-    Vec<E, R>::load(base + (0 * N + a) * nrhs, p0.v);
-    Vec<E, R>::load(base + (1 * N + a) * nrhs, p1.v);
-    Vec<E, R>::load(base + (u0p * N + a) * nrhs, q0.v);
-    Vec<E, R>::load(base + (u1p * N + a) * nrhs, q1.v);
+    Vec<E, R>::load(base + (0 * N + a) * cs, p0.v);
+    Vec<E, R>::load(base + (1 * N + a) * cs, p1.v);
+    Vec<E, R>::load(base + (u0p * N + a) * cs, q0.v);
+    Vec<E, R>::load(base + (u1p * N + a) * cs, q1.v);
     const T k0 = s * (T)gsign(MU, 0), k1 = s * (T)gsign(MU, 1);
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -249,8 +251,10 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 
 }  // namespace detail
 
-template <int P, int N, int R>
-__global__ void __launch_bounds__(256) wilson_mrhs_kernel(const DslashArgs A) {
+// MINB: minimum resident blocks of 256 threads per SM requested from the
+// compiler, i.e. a register cap of 65536 / (256 * MINB) per thread (1: 255).
+template <int P, int N, int R, int MINB>
+__global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs A) {
   using S = Store<P>;
   using T = typename S::real;
   using E = typename S::elem;
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(256) wilson_mrhs_kernel(const DslashArgs A) {
   for (int sp = 0; sp < 4; sp++)
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      const int64_t off = (site * 4 * N + sp * N + a) * nrhs + rhs0;
+      const int64_t off = ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0;
       if (xin) {
         VecBuf<E, R> xv;
         Vec<E, R>::load(xin + off, xv.v);
@@ -384,7 +388,7 @@ __global__ void __launch_bounds__(256) wilson_mrhs_kernel(const DslashArgs A) {
           float2 v = make_float2(acc[sp][a][r].x * inv[r], acc[sp][a][r].y * inv[r]);
           ov.v[r] = S::from_c(v);
         }
-        Vec<E, R>::store(out + (site * 4 * N + sp * N + a) * nrhs + rhs0, ov.v);
+        Vec<E, R>::store(out + ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0, ov.v);
       }
   } else {
 #pragma unroll
@@ -399,18 +403,18 @@ __global__ void __launch_bounds__(256) wilson_mrhs_kernel(const DslashArgs A) {
           e.y = acc[sp][a][r].y;
           ov.v[r] = e;
         }
-        Vec<E, R>::store(out + (site * 4 * N + sp * N + a) * nrhs + rhs0, ov.v);
+        Vec<E, R>::store(out + ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0, ov.v);
       }
   }
 }
 
 // host-side launcher of one instantiation
-template <int P, int N, int R>
+template <int P, int N, int R, int MINB>
 void launch_wilson_mrhs(const DslashArgs& A, int block, cudaStream_t stream) {
   const int groups = A.nrhs / R;
   const int64_t threads = (int64_t)A.geo.vh * groups;
   const int grid = (int)((threads + block - 1) / block);
-  wilson_mrhs_kernel<P, N, R><<<grid, block, 0, stream>>>(A);
+  wilson_mrhs_kernel<P, N, R, MINB><<<grid, block, 0, stream>>>(A);
 }
 
 }  // namespace qcu

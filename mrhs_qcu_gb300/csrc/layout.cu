@@ -48,7 +48,9 @@ __global__ void pack_fermions_kernel(PtrArray src, int mode, int parity, void* d
   double2 v[4 * N];
 #pragma unroll
   for (int c = 0; c < 4 * N; c++) v[c] = __ldg(s + c);
-  E* d = static_cast<E*>(dst) + (int64_t)site * 4 * N * nrhs + r;
+  // component-major MRHS field: component c at (c * Vh + site) * nrhs + r
+  const int64_t cs = (int64_t)g.vh * nrhs;
+  E* d = static_cast<E*>(dst) + (int64_t)site * nrhs + r;
   if constexpr (S::has_norm) {
     double m = 0.0;
 #pragma unroll
@@ -57,14 +59,14 @@ __global__ void pack_fermions_kernel(PtrArray src, int mode, int parity, void* d
     const double inv = m > 0.0 ? 1.0 / (double)mf : 0.0;
     dst_norm[(int64_t)site * nrhs + r] = mf;
 #pragma unroll
-    for (int c = 0; c < 4 * N; c++) d[(int64_t)c * nrhs] = S::from_c(make_float2((float)(v[c].x * inv), (float)(v[c].y * inv)));
+    for (int c = 0; c < 4 * N; c++) d[c * cs] = S::from_c(make_float2((float)(v[c].x * inv), (float)(v[c].y * inv)));
   } else {
 #pragma unroll
     for (int c = 0; c < 4 * N; c++) {
       E e;
       e.x = v[c].x;
       e.y = v[c].y;
-      d[(int64_t)c * nrhs] = e;
+      d[c * cs] = e;
     }
   }
 }
@@ -78,13 +80,14 @@ __global__ void unpack_fermions_kernel(PtrArray dstp, int mode, int parity, cons
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
   if ((int)site >= g.vh) return;
-  const E* s = static_cast<const E*>(src) + (int64_t)site * 4 * N * nrhs + r;
+  const int64_t cs = (int64_t)g.vh * nrhs;
+  const E* s = static_cast<const E*>(src) + (int64_t)site * nrhs + r;
   double2* d = static_cast<double2*>(const_cast<void*>(dstp.p[r])) + src_site(mode, site, parity, g) * (4 * N);
   double scale = 1.0;
   if constexpr (S::has_norm) scale = (double)src_norm[(int64_t)site * nrhs + r];
 #pragma unroll
   for (int c = 0; c < 4 * N; c++) {
-    auto v = S::to_c(s[(int64_t)c * nrhs]);
+    auto v = S::to_c(s[c * cs]);
     d[c] = make_double2((double)v.x * scale, (double)v.y * scale);
   }
 }
@@ -141,21 +144,23 @@ __global__ void convert_field_kernel(const void* src, const float* src_norm, voi
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
   if ((int64_t)site >= vh) return;
-  const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * ncomp * nrhs + r;
-  auto* d = static_cast<typename SO::elem*>(dst) + (int64_t)site * ncomp * nrhs + r;
+  // component-major: component c at (c * vh + site) * nrhs + r
+  const int64_t cs = vh * nrhs;
+  const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * nrhs + r;
+  auto* d = static_cast<typename SO::elem*>(dst) + (int64_t)site * nrhs + r;
   double si = 1.0;
   if constexpr (SI::has_norm) si = (double)src_norm[(int64_t)site * nrhs + r];
   double m = 0.0;
   if constexpr (SO::has_norm) {
     for (int c = 0; c < ncomp; c++) {
-      auto v = SI::to_c(s[(int64_t)c * nrhs]);
+      auto v = SI::to_c(s[c * cs]);
       m = fmax(m, fmax(fabs((double)v.x * si), fabs((double)v.y * si)));
     }
     dst_norm[(int64_t)site * nrhs + r] = (float)m;
   }
   const double inv = SO::has_norm ? (m > 0.0 ? 1.0 / (double)(float)m : 0.0) : 1.0;
   for (int c = 0; c < ncomp; c++) {
-    auto v = SI::to_c(s[(int64_t)c * nrhs]);
+    auto v = SI::to_c(s[c * cs]);
     const double re = (double)v.x * si * inv, im = (double)v.y * si * inv;
     typename SO::elem e;
     if constexpr (PO == PREC_DOUBLE) {
@@ -165,7 +170,7 @@ __global__ void convert_field_kernel(const void* src, const float* src_norm, voi
     } else {
       e = SO::from_c(make_float2((float)re, (float)im));
     }
-    d[(int64_t)c * nrhs] = e;
+    d[c * cs] = e;
   }
 }
 

@@ -360,7 +360,7 @@ int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_
   });
 }
 
-int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block) {
+int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks) {
   return guarded([&] {
     Session& s = session();
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -387,6 +387,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block) {
     qcu::DslashConfig c = s.tuner.tune(A, precision, s.N, s.stream());
     if (rhs_per_thread) *rhs_per_thread = c.R;
     if (block) *block = c.block;
+    if (min_blocks) *min_blocks = c.minb;
   });
 }
 

@@ -4,9 +4,11 @@
 //   gauge  [mu=4][parity=2][N*N][Vh] complex<P>   component-major per link,
 //          the reference's "coalesced" gauge order
 //          (include/basic_data/qcu_point.cuh:84-88 of the reference);
-//   fermion MRHS field [Vh][4N][nrhs] complex<P>, RHS innermost; for 16-bit
-//          storage an FP32 scale per (site, RHS) in a separate [Vh][nrhs]
-//          array, the stored values being component / scale.
+//   fermion MRHS field [4N][Vh][nrhs] complex<P>: component-major, RHS
+//          innermost, so a warp reading one component for consecutive sites
+//          reads one contiguous span; for 16-bit storage an FP32 scale per
+//          (site, RHS) in a separate [Vh][nrhs] array, the stored values being
+//          component / scale.
 // P is FP64 (double2), FP32 (float2), FP16 (__half2) or BF16 (__nv_bfloat162).
 #pragma once
 

@@ -55,11 +55,12 @@ void Autotuner::load_file() {
   if (!path) return;
   std::ifstream in(path);
   std::string k;
-  int R, block;
-  while (in >> k >> R >> block) {
+  int R, block, minb;
+  while (in >> k >> R >> block >> minb) {
     DslashConfig c;
     c.R = R;
     c.block = block;
+    c.minb = minb;
     cache_[k] = c;
   }
 }
@@ -68,16 +69,18 @@ void Autotuner::save_file() {
   const char* path = getenv("QCU_TUNE_CACHE");
   if (!path) return;
   std::ofstream out(path);
-  for (auto& kv : cache_) out << kv.first << " " << kv.second.R << " " << kv.second.block << "\n";
+  for (auto& kv : cache_)
+    out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
-  // QCU_DSLASH_CONFIG="R,block" pins the kernel shape (profiling, sweeps)
+  // QCU_DSLASH_CONFIG="R,block[,minb]" pins the kernel shape (profiling, sweeps)
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    if (sscanf(f, "%d,%d", &c.R, &c.block) == 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R) &&
-        c.block >= 32 && c.block <= 1024 && c.block % 32 == 0) {
+    const int got = sscanf(f, "%d,%d,%d", &c.R, &c.block, &c.minb);
+    if (got >= 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R, c.minb) && c.block >= 32 &&
+        c.block <= 256 && c.block % 32 == 0) {
       *found = true;
       return c;
     }
@@ -111,6 +114,11 @@ DslashConfig Autotuner::heuristic(int prec, int N, int nrhs) {
 }
 
 DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t st) {
+  if (getenv("QCU_DSLASH_CONFIG")) {
+    bool pinned = false;
+    DslashConfig c = lookup(prec, N, A.nrhs, A.geo.vh, &pinned);
+    if (pinned) return c;
+  }
   int opts[8];
   const int n = dslash_r_options(prec, N, opts, 8);
   const int blocks[] = {64, 128, 256};
@@ -121,23 +129,27 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   float best_ms = 1e30f;
   for (int i = 0; i < n; i++) {
     if (A.nrhs % opts[i]) continue;
-    for (int b : blocks) {
-      DslashConfig c;
-      c.R = opts[i];
-      c.block = b;
-      launch_dslash(A, prec, N, c, st);  // warm-up
-      QCU_CHECK_CUDA(cudaEventRecord(e0, st));
-      const int reps = 3;
-      for (int k = 0; k < reps; k++) launch_dslash(A, prec, N, c, st);
-      QCU_CHECK_CUDA(cudaEventRecord(e1, st));
-      QCU_CHECK_CUDA(cudaEventSynchronize(e1));
-      float ms = 0;
-      QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = c;
+    int minbs[8];
+    const int nm = dslash_minb_options(prec, N, opts[i], minbs, 8);
+    for (int j = 0; j < nm; j++)
+      for (int b : blocks) {
+        DslashConfig c;
+        c.R = opts[i];
+        c.block = b;
+        c.minb = minbs[j];
+        launch_dslash(A, prec, N, c, st);  // warm-up
+        QCU_CHECK_CUDA(cudaEventRecord(e0, st));
+        const int reps = 3;
+        for (int k = 0; k < reps; k++) launch_dslash(A, prec, N, c, st);
+        QCU_CHECK_CUDA(cudaEventRecord(e1, st));
+        QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = c;
+        }
       }
-    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

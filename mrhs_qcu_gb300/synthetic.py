@@ -85,3 +85,39 @@ def point_sources(L, n: int, nrhs: int, seed: int = 2) -> np.ndarray:
         col = int(rng.integers(n))
         b[r, p, site, spin, col] = 1.0
     return b
+
+
+def random_sun_torch(count: int, n: int, generator, device="cuda", chunk: int = 1 << 20):
+    """Haar-random SU(n) on a torch device with elementwise ops only (no
+    linear-algebra library): modified Gram-Schmidt of complex-Gaussian
+    columns (the phase-fixed QR), then division by det^(1/n), the
+    determinant from Gaussian elimination with partial pivoting."""
+    import torch
+    out = torch.empty((count, n, n), dtype=torch.complex128, device=device)
+    for s in range(0, count, chunk):
+        m = min(chunk, count - s)
+        re = torch.randn((m, n, n), generator=generator, device=device, dtype=torch.float64)
+        im = torch.randn((m, n, n), generator=generator, device=device, dtype=torch.float64)
+        q = torch.complex(re, im) * (0.5 ** 0.5)
+        for k in range(n):
+            v = q[:, :, k].clone()
+            for j in range(k):
+                qj = q[:, :, j]
+                v = v - (qj.conj() * v).sum(-1, keepdim=True) * qj
+            q[:, :, k] = v / v.abs().pow(2).sum(-1, keepdim=True).sqrt()
+        a = q.clone()
+        det = torch.ones(m, dtype=torch.complex128, device=device)
+        rows = torch.arange(m, device=device)
+        for k in range(n):
+            piv = a[:, k:, k].abs().argmax(dim=1) + k
+            swap = piv != k
+            rk = a[rows, k].clone()
+            rp = a[rows, piv].clone()
+            a[rows, k] = rp
+            a[rows, piv] = rk
+            det = torch.where(swap, -det, det) * a[:, k, k]
+            if k + 1 < n:
+                f = a[:, k + 1:, k] / a[:, k, k].unsqueeze(1)
+                a[:, k + 1:, :] -= f.unsqueeze(2) * a[:, k:k + 1, :]
+        out[s:s + m] = q * (det ** (-1.0 / n)).view(-1, 1, 1)
+    return out
