@@ -261,7 +261,7 @@ def run_gpu(args):
     nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
     Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
-    R, block, minb = Q.tune_dslash(nrhs, prec)
+    R, block, minb, pk = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
         Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
@@ -289,7 +289,7 @@ def run_gpu(args):
             "algorithmic_bytes_per_launch": bpu * units,
             "traffic": traffic.get("dram_bytes_per_launch")
             if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1) else None,
-            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d,MINB=%d> block %d" % (pname, R, minb, block),
+            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d,MINB=%d,PK=%d> block %d" % (pname, R, minb, pk, block),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 

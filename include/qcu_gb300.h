@@ -99,8 +99,9 @@ int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_
 
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
  * Returns the chosen RHS-per-thread, block size and register-cap variant
- * (minimum resident 256-thread blocks per SM). */
-int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *min_blocks);
+ * (minimum resident 256-thread blocks per SM) and whether the packed FP32x2
+ * arithmetic variant was chosen. */
+int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *min_blocks, int *packed);
 
 typedef struct QcuSolverParam_s {
   int solver;          /* QCU_SOLVER_CG or QCU_SOLVER_BICGSTAB */

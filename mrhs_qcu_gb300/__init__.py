@@ -116,7 +116,7 @@ def lib() -> ctypes.CDLL:
         "qcuEoToLex": ([P, P, I], I),
         "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
-        "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
     }
@@ -273,9 +273,10 @@ def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: 
 
 
 def tune_dslash(nrhs: int, precision: int):
-    R, B, M = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M)))
-    return R.value, B.value, M.value
+    R, B, M, K = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M),
+                                  ctypes.byref(K)))
+    return R.value, B.value, M.value, K.value
 
 
 def solver_params(**kw) -> QcuSolverParam:

@@ -14,25 +14,18 @@ std::mutex& registry_mutex() {
   static std::mutex m;
   return m;
 }
-int key(int prec, int N, int R, int minb) { return ((prec * 16 + N) * 16 + R) * 8 + minb; }
+int key(int prec, int N, int R, int minb, int pk) { return (((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk; }
 }  // namespace
 
-void register_dslash(int prec, int N, int R, int minb, DslashLauncher fn) {
+void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[key(prec, N, R, minb)] = fn;
+  registry()[key(prec, N, R, minb, pk)] = fn;
 }
 
-DslashLauncher find_dslash(int prec, int N, int R, int minb) {
+DslashLauncher find_dslash(int prec, int N, int R, int minb, int pk) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find(key(prec, N, R, minb));
+  auto it = registry().find(key(prec, N, R, minb, pk));
   return it == registry().end() ? nullptr : it->second;
-}
-
-int dslash_minb_options(int prec, int N, int R, int* out, int max) {
-  int n = 0;
-  for (int m = 1; m <= 7 && n < max; m++)
-    if (find_dslash(prec, N, R, m)) out[n++] = m;
-  return n;
 }
 
 int dslash_r_options(int prec, int N, int* out, int max) {
@@ -42,18 +35,31 @@ int dslash_r_options(int prec, int N, int* out, int max) {
   return n;
 }
 
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max) {
+  int n = 0;
+  for (int m = 1; m <= 7 && n < max; m++)
+    if (find_dslash(prec, N, R, m, pk)) out[n++] = m;
+  return n;
+}
+
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st) {
-  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb);
+  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk);
   QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
               std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +
-                  ", R=" + std::to_string(cfg.R) + ", minb=" + std::to_string(cfg.minb));
+                  ", R=" + std::to_string(cfg.R) + ", minb=" + std::to_string(cfg.minb) +
+                  ", pk=" + std::to_string(cfg.pk));
   QCU_REQUIRE(cfg.block >= 32 && cfg.block <= 256 && cfg.block % 32 == 0, QCU_ERR_INVALID_ARGUMENT,
               "dslash block size must be a multiple of 32 in 32..256");
   QCU_REQUIRE(A.nrhs % cfg.R == 0, QCU_ERR_INVALID_ARGUMENT, "nrhs not a multiple of R");
   QCU_REQUIRE((int64_t)A.geo.vh * (A.nrhs / cfg.R) < (1ll << 31), QCU_ERR_INVALID_ARGUMENT,
               "lattice x nrhs too large for one launch");
+  // the kernels index fields and links with 32-bit element offsets
+  QCU_REQUIRE((int64_t)4 * N * A.geo.vh * A.nrhs < (1ll << 32) && (int64_t)8 * N * N * A.geo.vh < (1ll << 32),
+              QCU_ERR_INVALID_ARGUMENT, "field too large for 32-bit element offsets");
   DslashArgs B = A;
   B.div_groups = FastDiv((uint32_t)(A.nrhs / cfg.R));
+  B.af = (float)A.a;
+  B.bf = (float)A.b;
   fn(B, cfg.block, st);
   QCU_CHECK_CUDA(cudaGetLastError());
 }

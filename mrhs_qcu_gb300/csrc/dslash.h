@@ -14,18 +14,20 @@ using DslashLauncher = void (*)(const DslashArgs&, int block, cudaStream_t);
 
 // registry filled by the instantiation units (dslash_inst_*.cu); minb is the
 // register-cap variant (minimum resident 256-thread blocks per SM)
-DslashLauncher find_dslash(int prec, int N, int R, int minb = 1);
-void register_dslash(int prec, int N, int R, int minb, DslashLauncher fn);
+// pk selects the packed FP32x2 arithmetic variant
+DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0);
+void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn);
 
 // RHS-per-thread values compiled for (prec, N), largest first
 int dslash_r_options(int prec, int N, int* out, int max);
-// register-cap variants compiled for (prec, N, R), ascending
-int dslash_minb_options(int prec, int N, int R, int* out, int max);
+// register-cap variants compiled for (prec, N, R, pk), ascending
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max);
 
 struct DslashConfig {
   int R = 1;
   int block = 128;  // <= 256 (launch bounds)
   int minb = 1;
+  int pk = 0;
 };
 
 // launch with an explicit configuration (throws if not compiled)

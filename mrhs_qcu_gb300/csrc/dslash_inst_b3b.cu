@@ -1,0 +1,13 @@
+// Dslash instances for PREC_BF16; registered at library load.
+#include "dslash.h"
+
+namespace qcu {
+namespace {
+struct Register_b3b {
+  Register_b3b() {
+    register_dslash(PREC_BF16, 3, 1, 3, 0, &launch_wilson_mrhs<PREC_BF16, 3, 1, 3, false>);
+    register_dslash(PREC_BF16, 3, 3, 1, 0, &launch_wilson_mrhs<PREC_BF16, 3, 3, 1, false>);
+  }
+} register_b3b;
+}  // namespace
+}  // namespace qcu

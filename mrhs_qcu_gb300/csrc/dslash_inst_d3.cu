@@ -5,11 +5,11 @@ namespace qcu {
 namespace {
 struct Register_d3 {
   Register_d3() {
-    register_dslash(PREC_DOUBLE, 3, 1, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 1>);
-    register_dslash(PREC_DOUBLE, 3, 1, 2, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 2>);
-    register_dslash(PREC_DOUBLE, 3, 2, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 2, 1>);
-    register_dslash(PREC_DOUBLE, 3, 3, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 3, 1>);
-    register_dslash(PREC_DOUBLE, 3, 4, 1, &launch_wilson_mrhs<PREC_DOUBLE, 3, 4, 1>);
+    register_dslash(PREC_DOUBLE, 3, 1, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 1, false>);
+    register_dslash(PREC_DOUBLE, 3, 1, 2, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 2, false>);
+    register_dslash(PREC_DOUBLE, 3, 2, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 2, 1, false>);
+    register_dslash(PREC_DOUBLE, 3, 3, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 3, 1, false>);
+    register_dslash(PREC_DOUBLE, 3, 4, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 4, 1, false>);
   }
 } register_d3;
 }  // namespace

@@ -5,15 +5,12 @@ namespace qcu {
 namespace {
 struct Register_s3 {
   Register_s3() {
-    register_dslash(PREC_SINGLE, 3, 1, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 1, 1>);
-    register_dslash(PREC_SINGLE, 3, 1, 2, &launch_wilson_mrhs<PREC_SINGLE, 3, 1, 2>);
-    register_dslash(PREC_SINGLE, 3, 1, 3, &launch_wilson_mrhs<PREC_SINGLE, 3, 1, 3>);
-    register_dslash(PREC_SINGLE, 3, 2, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 1>);
-    register_dslash(PREC_SINGLE, 3, 2, 2, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 2>);
-    register_dslash(PREC_SINGLE, 3, 3, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 3, 1>);
-    register_dslash(PREC_SINGLE, 3, 3, 2, &launch_wilson_mrhs<PREC_SINGLE, 3, 3, 2>);
-    register_dslash(PREC_SINGLE, 3, 4, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 4, 1>);
-    register_dslash(PREC_SINGLE, 3, 4, 2, &launch_wilson_mrhs<PREC_SINGLE, 3, 4, 2>);
+    register_dslash(PREC_SINGLE, 3, 1, 1, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 1, 1, false>);
+    register_dslash(PREC_SINGLE, 3, 1, 2, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 1, 2, false>);
+    register_dslash(PREC_SINGLE, 3, 2, 1, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 1, false>);
+    register_dslash(PREC_SINGLE, 3, 2, 2, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 2, false>);
+    register_dslash(PREC_SINGLE, 3, 4, 1, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 4, 1, false>);
+    register_dslash(PREC_SINGLE, 3, 2, 2, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 2, true>);
   }
 } register_s3;
 }  // namespace

@@ -36,6 +36,7 @@ struct DslashArgs {
   const float* x_norm;
   const int* mask;       // [nrhs] 0 = skip RHS, nullptr = all active
   double a, b;           // out = a * D in + b * x
+  float af, bf;          // a, b rounded once on the host for the FP32 kernels
   Geometry geo;
   int nrhs;
   int parity;            // output parity
@@ -57,10 +58,9 @@ __host__ __device__ constexpr int gsign(int mu, int r) {
                            : mu == 2 ? ((r == 0 || r == 3) ? 1 : -1) : 1;
 }
 
+// complex register type of the compute precision: float2 or double2
 template <typename T>
-struct C2 {
-  T x, y;
-};
+using C2 = typename cplx<T>::t;
 
 // Vector load/store of R consecutive storage elements (R RHS of one
 // component).  The offset is a multiple of R, so the widest vector whose size
@@ -141,11 +141,13 @@ __device__ __forceinline__ void load_norms(const float* p, float (&nrm)[R]) {
 //   s = -f (forward, projector 1 - f g) or +f (backward, 1 + f g)
 //   kup  = bc * scale_r        multiplies the two upper rows
 //   klo  = s * sign(lo) * bc * scale_r   the reconstructed lower rows
+// Offsets are 32-bit element indices into the field / gauge arrays (the host
+// checks that every array has fewer than 2^32 elements).
 template <int P, int N, int R, int MU, bool FWD>
 __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R], const DslashArgs& A,
                                    const typename Store<P>::elem* __restrict__ in,
-                                   const typename Store<P>::elem* __restrict__ gauge, int64_t link_base,
-                                   int64_t nb, int rhs0, typename Store<P>::real bc,
+                                   const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
+                                   uint32_t nb, uint32_t rhs0, typename Store<P>::real bc,
                                    typename Store<P>::real f) {
   using S = Store<P>;
   using T = typename S::real;
@@ -153,13 +155,13 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   constexpr int u0p = gperm(MU, 0), u1p = gperm(MU, 1);
   constexpr bool im = gimag(MU);
   const T s = FWD ? -f : f;
-  const int64_t vh = A.geo.vh;
-  const int nrhs = A.nrhs;
+  const uint32_t vh = (uint32_t)A.geo.vh;
+  const uint32_t nrhs = (uint32_t)A.nrhs;
 
   T scale[R];
   if constexpr (S::has_norm) {
     float nr[R];
-    load_norms<P, R>(A.in_norm + nb * nrhs + rhs0, nr);
+    load_norms<P, R>(A.in_norm + (nb * nrhs + rhs0), nr);
 #pragma unroll
     for (int r = 0; r < R; r++) scale[r] = bc * nr[r];
   } else {
@@ -170,15 +172,15 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   // project: h_u = psi_u + s g(u) psi_perm(u), u = 0, 1
   C2<T> h[2][N][R];
   // component-major field: component c of site nb at (c * Vh + nb) * nrhs
-  const int64_t cs = vh * nrhs;
-  const E* base = in + nb * nrhs + rhs0;
+  const uint32_t cs = vh * nrhs;
+  const uint32_t o = nb * nrhs + rhs0;
 #pragma unroll
   for (int a = 0; a < N; a++) {
     VecBuf<E, R> p0, p1, q0, q1;
-    Vec<E, R>::load(base + (0 * N + a) * cs, p0.v);
-    Vec<E, R>::load(base + (1 * N + a) * cs, p1.v);
-    Vec<E, R>::load(base + (u0p * N + a) * cs, q0.v);
-    Vec<E, R>::load(base + (u1p * N + a) * cs, q1.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(0 * N + a) * cs), p0.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(1 * N + a) * cs), p1.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(u0p * N + a) * cs), q0.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(u1p * N + a) * cs), q1.v);
     const T k0 = s * (T)gsign(MU, 0), k1 = s * (T)gsign(MU, 1);
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -212,8 +214,8 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 #pragma unroll
     for (int b = 0; b < N; b++) {
       // forward uses U[a][b]; backward uses conj(U[b][a])
-      const int comp = FWD ? (a * N + b) : (b * N + a);
-      auto uc = S::to_c(__ldg(gauge + link_base + (int64_t)comp * vh));
+      const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
+      auto uc = S::to_c(__ldg(gauge + (link_off + comp * vh)));
       const T ur = (T)uc.x;
       const T ui = FWD ? (T)uc.y : -(T)uc.y;
 #pragma unroll
@@ -249,22 +251,134 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   }
 }
 
+// The same hop for FP32 arithmetic on the packed FP32x2 pipe (sm_100+
+// fma.rn.f32x2 through __ffma2_rn): a complex multiply-add is two packed FMAs,
+//   t += (ur, ur) * (h.x, h.y) + (-ui, ui) * (h.y, h.x),
+// and the projection / reconstruction with real coefficients are one packed
+// FMA per complex number.  Same operation order per component as hop(), so
+// results agree to FP32 rounding.
+template <int P, int N, int R, int MU, bool FWD>
+__device__ __forceinline__ void hop_pk(float2 (&acc)[4][N][R], const DslashArgs& A,
+                                      const typename Store<P>::elem* __restrict__ in,
+                                      const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
+                                      uint32_t nb, uint32_t rhs0, float bc, float f) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  constexpr int u0p = gperm(MU, 0), u1p = gperm(MU, 1);
+  constexpr bool im = gimag(MU);
+  const float s = FWD ? -f : f;
+  const uint32_t vh = (uint32_t)A.geo.vh;
+  const uint32_t nrhs = (uint32_t)A.nrhs;
+
+  float scale[R];
+  if constexpr (S::has_norm) {
+    float nr[R];
+    load_norms<P, R>(A.in_norm + (nb * nrhs + rhs0), nr);
+#pragma unroll
+    for (int r = 0; r < R; r++) scale[r] = bc * nr[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < R; r++) scale[r] = bc;
+  }
+
+  float2 h[2][N][R], hs[2][N][R];  // hs = (h.y, h.x)
+  const uint32_t cs = vh * nrhs;
+  const uint32_t o = nb * nrhs + rhs0;
+  const float k0 = s * (float)gsign(MU, 0), k1 = s * (float)gsign(MU, 1);
+  const float2 K0 = im ? make_float2(-k0, k0) : make_float2(k0, k0);
+  const float2 K1 = im ? make_float2(-k1, k1) : make_float2(k1, k1);
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    VecBuf<E, R> p0, p1, q0, q1;
+    Vec<E, R>::load(in + (o + (uint32_t)(0 * N + a) * cs), p0.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(1 * N + a) * cs), p1.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(u0p * N + a) * cs), q0.v);
+    Vec<E, R>::load(in + (o + (uint32_t)(u1p * N + a) * cs), q1.v);
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 x0 = S::to_c(p0.v[r]), x1 = S::to_c(p1.v[r]);
+      const float2 y0 = S::to_c(q0.v[r]), y1 = S::to_c(q1.v[r]);
+      if constexpr (im) {  // h = x + k i y = (x.x - k y.y, x.y + k y.x)
+        h[0][a][r] = __ffma2_rn(K0, make_float2(y0.y, y0.x), x0);
+        h[1][a][r] = __ffma2_rn(K1, make_float2(y1.y, y1.x), x1);
+      } else {
+        h[0][a][r] = __ffma2_rn(K0, y0, x0);
+        h[1][a][r] = __ffma2_rn(K1, y1, x1);
+      }
+      hs[0][a][r] = make_float2(h[0][a][r].y, h[0][a][r].x);
+      hs[1][a][r] = make_float2(h[1][a][r].y, h[1][a][r].x);
+    }
+  }
+
+  const float klo0 = s * (float)gsign(MU, u0p), klo1 = s * (float)gsign(MU, u1p);
+#pragma unroll
+  for (int a = 0; a < N; a++) {
+    float2 t[2][R];
+#pragma unroll
+    for (int u = 0; u < 2; u++)
+#pragma unroll
+      for (int r = 0; r < R; r++) t[u][r] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int b = 0; b < N; b++) {
+      const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
+      const float2 uc = S::to_c(__ldg(gauge + (link_off + comp * vh)));
+      const float ui = FWD ? uc.y : -uc.y;
+      const float2 URR = make_float2(uc.x, uc.x), UII = make_float2(-ui, ui);
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          t[u][r] = __ffma2_rn(URR, h[u][b][r], t[u][r]);
+          t[u][r] = __ffma2_rn(UII, hs[u][b][r], t[u][r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 KU = make_float2(scale[r], scale[r]);
+      acc[0][a][r] = __ffma2_rn(KU, t[0][r], acc[0][a][r]);
+      acc[1][a][r] = __ffma2_rn(KU, t[1][r], acc[1][a][r]);
+      const float kl0 = klo0 * scale[r], kl1 = klo1 * scale[r];
+      if constexpr (im) {  // acc += kl i t = (-kl t.y, kl t.x)
+        acc[u0p][a][r] = __ffma2_rn(make_float2(-kl0, kl0), make_float2(t[0][r].y, t[0][r].x), acc[u0p][a][r]);
+        acc[u1p][a][r] = __ffma2_rn(make_float2(-kl1, kl1), make_float2(t[1][r].y, t[1][r].x), acc[u1p][a][r]);
+      } else {
+        acc[u0p][a][r] = __ffma2_rn(make_float2(kl0, kl0), t[0][r], acc[u0p][a][r]);
+        acc[u1p][a][r] = __ffma2_rn(make_float2(kl1, kl1), t[1][r], acc[u1p][a][r]);
+      }
+    }
+  }
+}
+
+template <int P, int N, int R, bool PK, int MU, bool FWD>
+__device__ __forceinline__ void hop_any(C2<typename Store<P>::real> (&acc)[4][N][R], const DslashArgs& A,
+                                       const typename Store<P>::elem* __restrict__ in,
+                                       const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
+                                       uint32_t nb, uint32_t rhs0, typename Store<P>::real bc,
+                                       typename Store<P>::real f) {
+  if constexpr (PK)
+    hop_pk<P, N, R, MU, FWD>(acc, A, in, gauge, link_off, nb, rhs0, bc, f);
+  else
+    hop<P, N, R, MU, FWD>(acc, A, in, gauge, link_off, nb, rhs0, bc, f);
+}
+
 }  // namespace detail
 
 // MINB: minimum resident blocks of 256 threads per SM requested from the
 // compiler, i.e. a register cap of 65536 / (256 * MINB) per thread (1: 255).
-template <int P, int N, int R, int MINB>
+// PK: FP32 arithmetic on the packed FP32x2 pipe (FP32 / 16-bit storage only).
+template <int P, int N, int R, int MINB, bool PK>
 __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs A) {
   using S = Store<P>;
   using T = typename S::real;
   using E = typename S::elem;
   using namespace detail;
+  static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
 
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t site_u, grp;
-  A.div_groups.divmod(gid, site_u, grp);
-  if ((int)site_u >= A.geo.vh) return;
-  const int rhs0 = (int)grp * R;
+  uint32_t site, grp;
+  A.div_groups.divmod(gid, site, grp);
+  if (site >= (uint32_t)A.geo.vh) return;
+  const uint32_t rhs0 = grp * R;
   if (A.mask) {
     bool any = false;
 #pragma unroll
@@ -272,20 +386,20 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
     if (!any) return;
   }
 
-  const int64_t site = site_u;
   uint32_t rest, xh, y, z, t;
-  A.geo.div_hx.divmod(site_u, rest, xh);
+  A.geo.div_hx.divmod(site, rest, xh);
   uint32_t rest2;
   A.geo.div_y.divmod(rest, rest2, y);
   A.geo.div_z.divmod(rest2, t, z);
-  const int hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
-  const int p = A.parity;
-  const int eo = (int)((y + z + t) & 1);
+  const uint32_t hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
+  const uint32_t p = A.parity;
+  const uint32_t eo = (y + z + t) & 1u;
   const T f = A.dagger ? (T)-1 : (T)1;
-  const int64_t vh = A.geo.vh;
+  const uint32_t vh = A.geo.vh;
+  const uint32_t nrhs = A.nrhs;
   const E* __restrict__ in = static_cast<const E*>(A.in);
   const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
-  constexpr int64_t NN = N * N;
+  constexpr uint32_t NN = N * N;
 
   C2<T> acc[4][N][R];
 #pragma unroll
@@ -295,53 +409,61 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
 #pragma unroll
       for (int r = 0; r < R; r++) acc[sp][a][r].x = acc[sp][a][r].y = (T)0;
 
-  // link bases: forward links at (mu, p, site), backward at (mu, 1-p, nb)
-  const int64_t lf = (int64_t)p * NN * vh + site;
-  const int64_t lb = (int64_t)(1 - p) * NN * vh;
+  // link offsets: forward links at (mu, p, site), backward at (mu, 1-p, nb)
+  const uint32_t lf = p * NN * vh + site;
+  const uint32_t lb = (1u - p) * NN * vh;
+  const uint32_t dmu = 2 * NN * vh;  // one direction's links
   {  // X
-    const int64_t nf = (eo != p) ? ((int)xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
-    const int64_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-    hop<P, N, R, 0, true>(acc, A, in, gauge, 0 * 2 * NN * vh + lf, nf, rhs0, (T)1, f);
-    hop<P, N, R, 0, false>(acc, A, in, gauge, 0 * 2 * NN * vh + lb + nbk, nbk, rhs0, (T)1, f);
+    const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+    const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+    hop_any<P, N, R, PK, 0, true>(acc, A, in, gauge, lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false>(acc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Y
-    const int64_t nf = ((int)y == Ly - 1) ? site - (int64_t)(Ly - 1) * hx : site + hx;
-    const int64_t nbk = (y == 0) ? site + (int64_t)(Ly - 1) * hx : site - hx;
-    hop<P, N, R, 1, true>(acc, A, in, gauge, 1 * 2 * NN * vh + lf, nf, rhs0, (T)1, f);
-    hop<P, N, R, 1, false>(acc, A, in, gauge, 1 * 2 * NN * vh + lb + nbk, nbk, rhs0, (T)1, f);
+    const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
+    const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
+    hop_any<P, N, R, PK, 1, true>(acc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false>(acc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Z
-    const int64_t pl = A.geo.plane;
-    const int64_t nf = ((int)z == Lz - 1) ? site - (int64_t)(Lz - 1) * pl : site + pl;
-    const int64_t nbk = (z == 0) ? site + (int64_t)(Lz - 1) * pl : site - pl;
-    hop<P, N, R, 2, true>(acc, A, in, gauge, 2 * 2 * NN * vh + lf, nf, rhs0, (T)1, f);
-    hop<P, N, R, 2, false>(acc, A, in, gauge, 2 * 2 * NN * vh + lb + nbk, nbk, rhs0, (T)1, f);
+    const uint32_t pl = A.geo.plane;
+    const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
+    const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
+    hop_any<P, N, R, PK, 2, true>(acc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false>(acc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // T, with the optional antiperiodic sign
-    const int64_t cb = A.geo.cube;
-    const bool top = (int)t == Lt - 1, bot = t == 0;
-    const int64_t nf = top ? site - (int64_t)(Lt - 1) * cb : site + cb;
-    const int64_t nbk = bot ? site + (int64_t)(Lt - 1) * cb : site - cb;
+    const uint32_t cb = A.geo.cube;
+    const bool top = t == Lt - 1, bot = t == 0;
+    const uint32_t nf = top ? site - (Lt - 1) * cb : site + cb;
+    const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
     const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
     const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
-    hop<P, N, R, 3, true>(acc, A, in, gauge, 3 * 2 * NN * vh + lf, nf, rhs0, bcf, f);
-    hop<P, N, R, 3, false>(acc, A, in, gauge, 3 * 2 * NN * vh + lb + nbk, nbk, rhs0, bcb, f);
+    hop_any<P, N, R, PK, 3, true>(acc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
+    hop_any<P, N, R, PK, 3, false>(acc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
   }
 
   // epilogue: out = a * acc + b * x
-  const int nrhs = A.nrhs;
-  const T ca = (T)A.a;
-  const T cbx = (T)A.b;
+  T ca, cbx;
+  if constexpr (sizeof(T) == 4) {
+    ca = A.af;
+    cbx = A.bf;
+  } else {
+    ca = (T)A.a;
+    cbx = (T)A.b;
+  }
   const E* __restrict__ xin = static_cast<const E*>(A.x);
   float xs[R];
   if constexpr (S::has_norm) {
-    if (xin) load_norms<P, R>(A.x_norm + site * nrhs + rhs0, xs);
+    if (xin) load_norms<P, R>(A.x_norm + (site * nrhs + rhs0), xs);
   }
+  const uint32_t cs = vh * nrhs;
+  const uint32_t o = site * nrhs + rhs0;
 #pragma unroll
   for (int sp = 0; sp < 4; sp++)
 #pragma unroll
     for (int a = 0; a < N; a++) {
-      const int64_t off = ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0;
+      const uint32_t off = o + (uint32_t)(sp * N + a) * cs;
       if (xin) {
         VecBuf<E, R> xv;
         Vec<E, R>::load(xin + off, xv.v);
@@ -377,7 +499,7 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
       inv[r] = m > 0.f ? 1.0f / m : 0.f;
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) A.out_norm[site * nrhs + rhs0 + r] = mx[r];
+    for (int r = 0; r < R; r++) A.out_norm[o + r] = mx[r];
 #pragma unroll
     for (int sp = 0; sp < 4; sp++)
 #pragma unroll
@@ -388,7 +510,7 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
           float2 v = make_float2(acc[sp][a][r].x * inv[r], acc[sp][a][r].y * inv[r]);
           ov.v[r] = S::from_c(v);
         }
-        Vec<E, R>::store(out + ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0, ov.v);
+        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v);
       }
   } else {
 #pragma unroll
@@ -403,18 +525,18 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
           e.y = acc[sp][a][r].y;
           ov.v[r] = e;
         }
-        Vec<E, R>::store(out + ((int64_t)(sp * N + a) * vh + site) * nrhs + rhs0, ov.v);
+        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v);
       }
   }
 }
 
 // host-side launcher of one instantiation
-template <int P, int N, int R, int MINB>
+template <int P, int N, int R, int MINB, bool PK = false>
 void launch_wilson_mrhs(const DslashArgs& A, int block, cudaStream_t stream) {
   const int groups = A.nrhs / R;
   const int64_t threads = (int64_t)A.geo.vh * groups;
   const int grid = (int)((threads + block - 1) / block);
-  wilson_mrhs_kernel<P, N, R, MINB><<<grid, block, 0, stream>>>(A);
+  wilson_mrhs_kernel<P, N, R, MINB, PK><<<grid, block, 0, stream>>>(A);
 }
 
 }  // namespace qcu

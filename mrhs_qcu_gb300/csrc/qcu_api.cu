@@ -360,7 +360,7 @@ int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_
   });
 }
 
-int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks) {
+int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed) {
   return guarded([&] {
     Session& s = session();
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -388,6 +388,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (rhs_per_thread) *rhs_per_thread = c.R;
     if (block) *block = c.block;
     if (min_blocks) *min_blocks = c.minb;
+    if (packed) *packed = c.pk;
   });
 }
 

@@ -55,12 +55,13 @@ void Autotuner::load_file() {
   if (!path) return;
   std::ifstream in(path);
   std::string k;
-  int R, block, minb;
-  while (in >> k >> R >> block >> minb) {
+  int R, block, minb, pk;
+  while (in >> k >> R >> block >> minb >> pk) {
     DslashConfig c;
     c.R = R;
     c.block = block;
     c.minb = minb;
+    c.pk = pk;
     cache_[k] = c;
   }
 }
@@ -70,7 +71,8 @@ void Autotuner::save_file() {
   if (!path) return;
   std::ofstream out(path);
   for (auto& kv : cache_)
-    out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << "\n";
+    out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << " " << kv.second.pk
+        << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
@@ -78,8 +80,8 @@ DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   // QCU_DSLASH_CONFIG="R,block[,minb]" pins the kernel shape (profiling, sweeps)
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    const int got = sscanf(f, "%d,%d,%d", &c.R, &c.block, &c.minb);
-    if (got >= 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R, c.minb) && c.block >= 32 &&
+    const int got = sscanf(f, "%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk);
+    if (got >= 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R, c.minb, c.pk) && c.block >= 32 &&
         c.block <= 256 && c.block % 32 == 0) {
       *found = true;
       return c;
@@ -129,14 +131,16 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   float best_ms = 1e30f;
   for (int i = 0; i < n; i++) {
     if (A.nrhs % opts[i]) continue;
+    for (int pk = 0; pk < 2; pk++) {
     int minbs[8];
-    const int nm = dslash_minb_options(prec, N, opts[i], minbs, 8);
+    const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8);
     for (int j = 0; j < nm; j++)
       for (int b : blocks) {
         DslashConfig c;
         c.R = opts[i];
         c.block = b;
         c.minb = minbs[j];
+        c.pk = pk;
         launch_dslash(A, prec, N, c, st);  // warm-up
         QCU_CHECK_CUDA(cudaEventRecord(e0, st));
         const int reps = 3;
@@ -150,6 +154,7 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
           best = c;
         }
       }
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
