@@ -97,6 +97,13 @@ int qcuDslashMRHS(void *out, void *out_norm, const void *in, const void *in_norm
 int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_norm, const void *x,
                       const void *x_norm, int nrhs, int parity, int dagger, int precision, double a, double b);
 
+/* out[r] = |field_r|^2 (FP64 accumulation, deterministic order) for each RHS
+ * of a resident MRHS field of the session lattice, precision FP32 or FP64.
+ * out is a device array of nrhs doubles.  The block partial sums live in the
+ * session's workspace (allocated on first use).  Asynchronous on the library
+ * stream. */
+int qcuNorm2MRHS(double *out, const void *field, int precision, int nrhs);
+
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
  * Returns the chosen RHS-per-thread, block size and register-cap variant
  * (minimum resident 256-thread blocks per SM) and whether the packed FP32x2

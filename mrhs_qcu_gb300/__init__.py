@@ -73,7 +73,7 @@ ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge"
 EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
-               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert"]
+               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS"]
 # C++ symbols with the reference's mangled names (include/qcu_storage.h)
 CXX_SYMBOLS = ["_ZN3qcu7storage18shiftVectorStorageEPvS1_14ShiftDirectioniiii",
                "_ZN3qcu7storage17shiftGaugeStorageEPvS1_14ShiftDirectioniiii"]
@@ -119,6 +119,7 @@ def lib() -> ctypes.CDLL:
         "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
+        "qcuNorm2MRHS": ([P, P, I, I], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -270,6 +271,11 @@ def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: 
                      a: float, b: float) -> None:
     _raise_if(lib().qcuDslashXpayMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), _p(x), _p(x_norm), int(nrhs),
                                       int(parity), int(dagger), int(precision), float(a), float(b)))
+
+
+def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:
+    """out[r] = |field_r|^2 into a device array of nrhs doubles (qcuNorm2MRHS)."""
+    _raise_if(lib().qcuNorm2MRHS(_p(out), _p(field), int(precision), int(nrhs)))
 
 
 def tune_dslash(nrhs: int, precision: int):

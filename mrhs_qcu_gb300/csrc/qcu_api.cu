@@ -360,6 +360,22 @@ int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_
   });
 }
 
+int qcuNorm2MRHS(double* out, const void* field, int precision, int nrhs) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(out && field, QCU_ERR_INVALID_ARGUMENT, "null pointer");
+    QCU_REQUIRE(precision == QCU_SINGLE_PRECISION || precision == QCU_DOUBLE_PRECISION, QCU_ERR_UNSUPPORTED,
+                "norms are computed for FP32 or FP64 fields");
+    QCU_REQUIRE(nrhs >= 1 && nrhs <= qcu::QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
+    qcu::FieldRef f;
+    f.data = const_cast<void*>(field);
+    f.prec = precision;
+    f.nrhs = nrhs;
+    f.n = (int64_t)s.field_elems(nrhs);
+    s.blas().norm2(f, out, s.stream());
+  });
+}
+
 int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed) {
   return guarded([&] {
     Session& s = session();
