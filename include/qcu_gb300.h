@@ -104,6 +104,24 @@ int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_
  * stream. */
 int qcuNorm2MRHS(double *out, const void *field, int precision, int nrhs);
 
+/* No counterpart in the reference.  The same per-RHS norm for callers that
+ * cannot allocate device memory: host callbacks and graph nodes, real-time
+ * loops that cannot absorb cudaFree's device-wide synchronisation, processes
+ * whose device memory another allocator already owns.  It needs no session
+ * and allocates nothing.  The block partial sums live in a fixed 512 KiB
+ * array inside libqcu.so, held on every GPU that loads the library until the
+ * process exits.
+ *   field:      n_elements complex values, RHS innermost (element e belongs
+ *               to RHS e % nrhs), FP32 or FP64
+ *   out:        device array of nrhs doubles
+ *   limit:      nrhs <= 64; larger requests return QCU_ERR_CAPACITY
+ *   stream:     cudaStream_t (NULL: the legacy default stream), asynchronous
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call shares the one array: calls whose work overlaps on the GPU
+ * race, so serialise them (one stream, or events). */
+int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_elements, int nrhs, void *stream);
+
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
  * Returns the chosen RHS-per-thread, block size and register-cap variant
  * (minimum resident 256-thread blocks per SM) and whether the packed FP32x2

@@ -73,7 +73,7 @@ ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge"
 EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
-               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS"]
+               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS", "qcuNorm2MRHSNoAlloc"]
 # C++ symbols with the reference's mangled names (include/qcu_storage.h)
 CXX_SYMBOLS = ["_ZN3qcu7storage18shiftVectorStorageEPvS1_14ShiftDirectioniiii",
                "_ZN3qcu7storage17shiftGaugeStorageEPvS1_14ShiftDirectioniiii"]
