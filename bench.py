@@ -361,6 +361,11 @@ def run_gpu(args):
     if rank == 0 and not args.skip_solve:
         solve = solve_bench(torch, Q)
 
+    # ---- serving stream: continuous batching over resident gauges -------
+    serve = None
+    if rank == 0 and not args.skip_serve:
+        serve = serve_bench(torch, Q)
+
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -372,7 +377,7 @@ def run_gpu(args):
                        "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
             "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
-            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "solve": solve,
+            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "solve": solve, "serve": serve,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -437,6 +442,89 @@ def solve_bench(torch, Q):
     return out
 
 
+def serve_bench(torch, Q, n_requests=48, rate=60.0, serial_budget_s=8.0):
+    """Serving stream: seeded Poisson arrivals into a server with 4 resident
+    gauges; p50/p99 latency and solves/s, next to serial plain-FP64 solves of
+    the same requests (one at a time, a bounded sample)."""
+    from mrhs_qcu_gb300 import synthetic as S
+    gauges = [((8, 8, 8, 8), 3), ((16, 16, 16, 32), 3), ((24, 24, 24, 48), 3), ((16, 16, 16, 32), 4)]
+    srv = Q.Server(160 << 30, max_slots=24, inner_precision=Q.QCU_SINGLE_PRECISION)
+    dgs = []
+    for gid, (L, n) in enumerate(gauges):
+        g, _ = make_inputs(torch, L, n, 1, seed_g=100 + gid)
+        dgs.append(g)
+        srv.add_gauge(gid, L, n, g.data_ptr(), antiperiodic_t=True)
+    rng = np.random.default_rng(7)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    reqs = []
+    for i in range(n_requests):
+        gid = int(rng.integers(len(gauges)))
+        L, n = gauges[gid]
+        nrhs = int(rng.integers(1, 25))
+        kappa = float(rng.uniform(0.10, 0.125))
+        tol = float(rng.choice([1e-8, 1e-10, 1e-12]))
+        vh = S.half_volume(L)
+        gen = torch.Generator(device="cuda").manual_seed(1000 + i)
+        b = torch.complex(torch.randn((nrhs, 2, vh, 4, n), generator=gen, device="cuda", dtype=torch.float64),
+                          torch.randn((nrhs, 2, vh, 4, n), generator=gen, device="cuda", dtype=torch.float64))
+        x = torch.zeros_like(b)
+        reqs.append((gid, kappa, tol, b, x))
+    torch.cuda.synchronize()
+    # warm-up: one request per gauge (kernel tuning, graph capture)
+    for gid, (L, n) in enumerate(gauges):
+        vh = S.half_volume(L)
+        b = torch.ones((1, 2, vh, 4, n), dtype=torch.complex128, device="cuda")
+        x = torch.zeros_like(b)
+        srv.wait(srv.submit(gid, 0.11, 1e-8, [x[0].data_ptr()], [b[0].data_ptr()]))
+    base = srv.stats().completed
+    ids = []
+    t0 = time.perf_counter()
+    for (gid, kappa, tol, b, x), t_arr in zip(reqs, arrivals):
+        delay = t_arr - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(gid, kappa, tol, [x[r].data_ptr() for r in range(x.shape[0])],
+                              [b[r].data_ptr() for r in range(b.shape[0])]))
+    infos = [srv.wait(i) for i in ids]
+    wall = time.perf_counter() - t0
+    lat = sorted(inf.latency_s for inf in infos)
+    ok = all(inf.status == 0 for inf in infos)
+    worst = max(inf.max_true_residual / reqs[k][2] for k, inf in enumerate(infos))
+    out = {"workload": "%d requests, Poisson %.0f req/s, 4 resident gauges (8^4, 16^3x32, 24^3x48 SU(3); 16^3x32 "
+                       "SU(4)), nrhs U[1,24], kappa U[0.10,0.125], tol {1e-8,1e-10,1e-12}, FP32 inner + FP64 "
+                       "reliable updates" % (n_requests, rate),
+           "p50_s": round(float(np.percentile(lat, 50)), 4), "p99_s": round(float(np.percentile(lat, 99)), 4),
+           "mean_s": round(float(np.mean(lat)), 4), "solves_per_s": round(n_requests / wall, 2),
+           "rhs_per_s": round(sum(r[3].shape[0] for r in reqs) / wall, 1), "wall_s": round(wall, 3),
+           "all_ok": bool(ok), "max_true_residual_over_tol": worst,
+           "completed": srv.stats().completed - base}
+    srv.close()
+    # serial plain FP64: each request alone through qcuInvert, a bounded sample
+    t_ser, n_ser = 0.0, 0
+    cur = None
+    for gid, kappa, tol, b, x in reqs:
+        if t_ser > serial_budget_s:
+            break
+        L, n = gauges[gid]
+        if cur != gid:
+            Q.initGridSize(L, n)
+            Q.set_antiperiodic_t(True)
+            Q.loadQcuGauge(dgs[gid].data_ptr())
+            cur = gid
+        x.zero_()
+        p = Q.solver_params(kappa=kappa, tol=tol, inner_precision=Q.QCU_DOUBLE_PRECISION, max_iter=20000)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        Q.invert([x[r].data_ptr() for r in range(x.shape[0])], [b[r].data_ptr() for r in range(b.shape[0])], p,
+                 raise_on_error=False)
+        torch.cuda.synchronize()
+        t_ser += time.perf_counter() - t1
+        n_ser += 1
+    out["serial_fp64_solves_per_s"] = round(n_ser / t_ser, 2) if t_ser > 0 else None
+    out["serial_fp64_sample"] = "%d of the %d requests, one at a time, plain FP64 CG" % (n_ser, n_requests)
+    return out
+
+
 def run_reference(args):
     """The reference's CPU path for this operator: FP64 OpenMP restatement
     (the reference itself has no CPU implementation), all host threads."""
@@ -477,6 +565,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-sweep", action="store_true")
     ap.add_argument("--skip-solve", action="store_true")
+    ap.add_argument("--skip-serve", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -487,7 +576,7 @@ def main():
                     help="headline kernel only (no e2e, sweep, CPU or solve legs), for ncu captures")
     args = ap.parse_args()
     if args.profile:
-        args.skip_sweep = args.skip_solve = args.skip_cpu = args.skip_e2e = True
+        args.skip_sweep = args.skip_solve = args.skip_serve = args.skip_cpu = args.skip_e2e = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

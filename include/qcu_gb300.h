@@ -128,6 +128,12 @@ int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_
  * arithmetic variant was chosen. */
 int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *min_blocks, int *packed);
 
+/* The compiled dslash kernel shapes for (precision, nColors): *count triples
+ * (RHS per thread, min_blocks, packed) are available; the first max_shapes
+ * are written to shapes[3 * i .. 3 * i + 2].  Any of them can be pinned with
+ * QCU_DSLASH_CONFIG="R,block,min_blocks,packed". */
+int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
+
 typedef struct QcuSolverParam_s {
   int solver;          /* QCU_SOLVER_CG or QCU_SOLVER_BICGSTAB */
   int inner_precision; /* operator precision of the inner iterations */
@@ -144,6 +150,46 @@ typedef struct QcuSolverParam_s {
   double true_residual[256]; /* per RHS, FP64 */
   int converged[256];
 } QcuSolverParam;
+
+/* ---- solve server: resident gauges, continuous MRHS batching ------------
+ * A server keeps gauge fields resident (one lane each, with its own stream
+ * and worker thread, so lanes overlap on the device), admits requests into
+ * free RHS slots between iteration chunks of the running batch, and reports
+ * latency percentiles.  A lane's slot capacity is fixed when its gauge is
+ * added, from the HBM budget.  Requests carry their own kappa and tolerance;
+ * x and b are device arrays of nrhs full even-odd fields [2][Vh][4][N]
+ * (complex double) that must stay valid until the request is done.  The
+ * server calls are thread-safe and do not use the qcu.h session.  Lanes run
+ * on non-blocking streams of their own; work queued on the legacy default
+ * stream before qcuServerAddGauge / qcuServerSubmit is ordered before the
+ * server reads the gauge / the sources, and a request's solution is in
+ * memory when qcuServerWait reports it done. */
+typedef struct QcuRequestInfo_s {
+  int done, status, nrhs, iterations;
+  double latency_s; /* submit -> solution written */
+  double queue_s;   /* submit -> admitted */
+  double max_true_residual;
+  int all_converged;
+} QcuRequestInfo;
+
+typedef struct QcuServerStats_s {
+  long long submitted, completed;
+  double p50_s, p99_s, mean_s;
+  double solves_per_s, rhs_per_s;
+  size_t hbm_used;
+} QcuServerStats;
+
+int qcuServerCreate(void **server, size_t hbm_budget_bytes, int max_slots_per_gauge, int inner_precision,
+                    int solver);
+int qcuServerAddGauge(void *server, int gauge_id, const int lattice[4], int nColors, const void *gauge,
+                      int antiperiodic_t);
+int qcuServerSubmit(void *server, int gauge_id, double kappa, double tol, int nrhs, void *const *x,
+                    void *const *b, long long *request_id);
+/* timeout < 0 waits forever; returns QCU_OK whether or not the request is done
+ * (see info->done and info->status) */
+int qcuServerWait(void *server, long long request_id, double timeout_s, QcuRequestInfo *info);
+int qcuServerStats(void *server, QcuServerStats *stats);
+int qcuServerDestroy(void *server);
 
 void qcuSolverParamDefaults(QcuSolverParam *p);
 /* Solve M x_r = b_r for nrhs right-hand sides with the loaded gauge. */

@@ -73,7 +73,22 @@ ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge"
 EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
-               "qcuTuneDslash", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS", "qcuNorm2MRHSNoAlloc"]
+               "qcuTuneDslash", "qcuDslashKernels", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
+               "qcuNorm2MRHSNoAlloc",
+               "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
+               "qcuServerDestroy"]
+
+
+class QcuRequestInfo(ctypes.Structure):
+    _fields_ = [("done", ctypes.c_int), ("status", ctypes.c_int), ("nrhs", ctypes.c_int),
+                ("iterations", ctypes.c_int), ("latency_s", ctypes.c_double), ("queue_s", ctypes.c_double),
+                ("max_true_residual", ctypes.c_double), ("all_converged", ctypes.c_int)]
+
+
+class QcuServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("p50_s", ctypes.c_double),
+                ("p99_s", ctypes.c_double), ("mean_s", ctypes.c_double), ("solves_per_s", ctypes.c_double),
+                ("rhs_per_s", ctypes.c_double), ("hbm_used", ctypes.c_size_t)]
 # C++ symbols with the reference's mangled names (include/qcu_storage.h)
 CXX_SYMBOLS = ["_ZN3qcu7storage18shiftVectorStorageEPvS1_14ShiftDirectioniiii",
                "_ZN3qcu7storage17shiftGaugeStorageEPvS1_14ShiftDirectioniiii"]
@@ -117,9 +132,17 @@ def lib() -> ctypes.CDLL:
         "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
         "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
         "qcuNorm2MRHS": ([P, P, I, I], I),
+        "qcuNorm2MRHSNoAlloc": ([P, P, I, S, I, P], I),
+        "qcuServerCreate": ([ctypes.POINTER(ctypes.c_void_p), S, I, I, I], I),
+        "qcuServerAddGauge": ([P, I, ctypes.POINTER(I), I, P, I], I),
+        "qcuServerSubmit": ([P, I, D, D, I, PP, PP, ctypes.POINTER(ctypes.c_longlong)], I),
+        "qcuServerWait": ([P, ctypes.c_longlong, D, ctypes.POINTER(QcuRequestInfo)], I),
+        "qcuServerStats": ([P, ctypes.POINTER(QcuServerStats)], I),
+        "qcuServerDestroy": ([P], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -285,6 +308,14 @@ def tune_dslash(nrhs: int, precision: int):
     return R.value, B.value, M.value, K.value
 
 
+def dslash_kernels(precision: int, n_colors: int = 3):
+    """Compiled dslash kernel shapes [(R, min_blocks, packed), ...]."""
+    arr = (ctypes.c_int * (3 * 64))()
+    cnt = ctypes.c_int()
+    _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
+    return [tuple(arr[3 * i:3 * i + 3]) for i in range(min(cnt.value, 64))]
+
+
 def solver_params(**kw) -> QcuSolverParam:
     p = QcuSolverParam()
     lib().qcuSolverParamDefaults(ctypes.byref(p))
@@ -302,3 +333,53 @@ def invert(xs, bs, params: QcuSolverParam, raise_on_error: bool = True) -> QcuSo
     else:
         clear_error()
     return params
+
+
+class Server:
+    """Solve server (qcuServer*): resident gauge fields, HBM-budget admission,
+    continuous MRHS batching, p50/p99 latency."""
+
+    def __init__(self, hbm_budget_bytes: int, max_slots: int = 24, inner_precision: int = QCU_SINGLE_PRECISION,
+                 solver: int = QCU_SOLVER_CG):
+        h = ctypes.c_void_p()
+        _raise_if(lib().qcuServerCreate(ctypes.byref(h), int(hbm_budget_bytes), int(max_slots),
+                                        int(inner_precision), int(solver)))
+        self.h = h
+        self._keep = {}
+
+    def add_gauge(self, gauge_id: int, lattice, n_colors: int, gauge_ptr, antiperiodic_t: bool = False) -> None:
+        L = (ctypes.c_int * 4)(*[int(v) for v in lattice])
+        _raise_if(lib().qcuServerAddGauge(self.h, int(gauge_id), L, int(n_colors), _p(gauge_ptr),
+                                          int(bool(antiperiodic_t))))
+
+    def submit(self, gauge_id: int, kappa: float, tol: float, xs, bs) -> int:
+        px, kx = _ptrs(xs)
+        pb, kb = _ptrs(bs)
+        rid = ctypes.c_longlong()
+        _raise_if(lib().qcuServerSubmit(self.h, int(gauge_id), float(kappa), float(tol), len(xs), px, pb,
+                                        ctypes.byref(rid)))
+        self._keep[rid.value] = (kx, kb)
+        return rid.value
+
+    def wait(self, request_id: int, timeout_s: float = -1.0) -> QcuRequestInfo:
+        info = QcuRequestInfo()
+        _raise_if(lib().qcuServerWait(self.h, ctypes.c_longlong(request_id), float(timeout_s), ctypes.byref(info)))
+        if info.done:
+            self._keep.pop(request_id, None)
+        return info
+
+    def stats(self) -> QcuServerStats:
+        st = QcuServerStats()
+        _raise_if(lib().qcuServerStats(self.h, ctypes.byref(st)))
+        return st
+
+    def close(self) -> None:
+        if self.h:
+            _raise_if(lib().qcuServerDestroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

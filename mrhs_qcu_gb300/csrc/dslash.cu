@@ -56,6 +56,8 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
   // the kernels index fields and links with 32-bit element offsets
   QCU_REQUIRE((int64_t)4 * N * A.geo.vh * A.nrhs < (1ll << 32) && (int64_t)8 * N * N * A.geo.vh < (1ll << 32),
               QCU_ERR_INVALID_ARGUMENT, "field too large for 32-bit element offsets");
+  QCU_REQUIRE((int64_t)A.geo.vh * A.nrhs * prec_complex_bytes(prec) < (1ll << 32), QCU_ERR_INVALID_ARGUMENT,
+              "field component stride must stay below 4 GB");
   DslashArgs B = A;
   B.div_groups = FastDiv((uint32_t)(A.nrhs / cfg.R));
   B.af = (float)A.a;

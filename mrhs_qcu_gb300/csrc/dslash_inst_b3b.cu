@@ -7,6 +7,8 @@ struct Register_b3b {
   Register_b3b() {
     register_dslash(PREC_BF16, 3, 1, 3, 0, &launch_wilson_mrhs<PREC_BF16, 3, 1, 3, false>);
     register_dslash(PREC_BF16, 3, 3, 1, 0, &launch_wilson_mrhs<PREC_BF16, 3, 3, 1, false>);
+    register_dslash(PREC_BF16, 3, 2, 2, 1, &launch_wilson_mrhs<PREC_BF16, 3, 2, 2, true>);
+    register_dslash(PREC_BF16, 3, 4, 1, 1, &launch_wilson_mrhs<PREC_BF16, 3, 4, 1, true>);
   }
 } register_b3b;
 }  // namespace

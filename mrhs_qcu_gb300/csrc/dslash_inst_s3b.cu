@@ -9,6 +9,7 @@ struct Register_s3b {
     register_dslash(PREC_SINGLE, 3, 3, 1, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 3, 1, false>);
     register_dslash(PREC_SINGLE, 3, 3, 2, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 3, 2, false>);
     register_dslash(PREC_SINGLE, 3, 4, 2, 0, &launch_wilson_mrhs<PREC_SINGLE, 3, 4, 2, false>);
+    register_dslash(PREC_SINGLE, 3, 2, 1, 1, &launch_wilson_mrhs<PREC_SINGLE, 3, 2, 1, true>);
   }
 } register_s3b;
 }  // namespace

@@ -37,6 +37,8 @@ struct DslashArgs {
   const int* mask;       // [nrhs] 0 = skip RHS, nullptr = all active
   double a, b;           // out = a * D in + b * x
   float af, bf;          // a, b rounded once on the host for the FP32 kernels
+  const float* a_rhs_f;  // optional per-RHS a (replaces a) for FP32 arithmetic
+  const double* a_rhs_d; // optional per-RHS a for FP64 arithmetic
   Geometry geo;
   int nrhs;
   int parity;            // output parity
@@ -171,16 +173,18 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 
   // project: h_u = psi_u + s g(u) psi_perm(u), u = 0, 1
   C2<T> h[2][N][R];
-  // component-major field: component c of site nb at (c * Vh + nb) * nrhs
-  const uint32_t cs = vh * nrhs;
-  const uint32_t o = nb * nrhs + rhs0;
+  // component-major field: component c of site nb at (c * Vh + nb) * nrhs.
+  // One 64-bit base per hop; each component is then base + c * stride with a
+  // compile-time c (a single wide multiply-add per address).
+  const uint32_t cs_bytes = vh * nrhs * (uint32_t)sizeof(E);
+  const char* base = reinterpret_cast<const char*>(in + (nb * nrhs + rhs0));
 #pragma unroll
   for (int a = 0; a < N; a++) {
     VecBuf<E, R> p0, p1, q0, q1;
-    Vec<E, R>::load(in + (o + (uint32_t)(0 * N + a) * cs), p0.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(1 * N + a) * cs), p1.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(u0p * N + a) * cs), q0.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(u1p * N + a) * cs), q1.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(0 * N + a) * cs_bytes), p0.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(1 * N + a) * cs_bytes), p1.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u0p * N + a) * cs_bytes), q0.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u1p * N + a) * cs_bytes), q1.v);
     const T k0 = s * (T)gsign(MU, 0), k1 = s * (T)gsign(MU, 1);
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -202,7 +206,10 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
     }
   }
 
-  // colour multiply row by row, then reconstruct
+  // colour multiply row by row, then reconstruct; link component k at
+  // lbase + k * ls_bytes
+  const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
+  const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);
   const T klo0 = s * (T)gsign(MU, u0p), klo1 = s * (T)gsign(MU, u1p);
 #pragma unroll
   for (int a = 0; a < N; a++) {
@@ -215,7 +222,7 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
     for (int b = 0; b < N; b++) {
       // forward uses U[a][b]; backward uses conj(U[b][a])
       const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
-      auto uc = S::to_c(__ldg(gauge + (link_off + comp * vh)));
+      auto uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp * ls_bytes)));
       const T ur = (T)uc.x;
       const T ui = FWD ? (T)uc.y : -(T)uc.y;
 #pragma unroll
@@ -251,21 +258,26 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   }
 }
 
-// The same hop for FP32 arithmetic on the packed FP32x2 pipe (sm_100+
-// fma.rn.f32x2 through __ffma2_rn): a complex multiply-add is two packed FMAs,
-//   t += (ur, ur) * (h.x, h.y) + (-ui, ui) * (h.y, h.x),
-// and the projection / reconstruction with real coefficients are one packed
-// FMA per complex number.  Same operation order per component as hop(), so
-// results agree to FP32 rounding.
+// The same hop with FP32 arithmetic on the packed FP32x2 pipe (sm_100+
+// fma.rn.f32x2 through __ffma2_rn).  The two lanes of a packed register hold
+// the two projected spin rows u = 0, 1, which the SU(N) multiply scales by
+// the same link element:
+//   t_re(u=0,1) += (ur, ur) * h_re(u=0,1) + (-ui, -ui) * h_im(u=0,1)
+//   t_im(u=0,1) += (ur, ur) * h_im(u=0,1) + ( ui,  ui) * h_re(u=0,1)
+// so one complex multiply-add of both rows is four packed FMAs instead of
+// eight.  The accumulator is kept in the same lane order: pair s holds spin
+// rows (2s, 2s+1), real parts in re[s], imaginary parts in im[s].  Every
+// lane performs exactly the FMA sequence of hop(), so the results are
+// bit-identical to it.
 template <int P, int N, int R, int MU, bool FWD>
-__device__ __forceinline__ void hop_pk(float2 (&acc)[4][N][R], const DslashArgs& A,
-                                      const typename Store<P>::elem* __restrict__ in,
-                                      const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
-                                      uint32_t nb, uint32_t rhs0, float bc, float f) {
+__device__ __forceinline__ void hop_pk(float2 (&re)[2][N][R], float2 (&im)[2][N][R], const DslashArgs& A,
+                                       const typename Store<P>::elem* __restrict__ in,
+                                       const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
+                                       uint32_t nb, uint32_t rhs0, float bc, float f) {
   using S = Store<P>;
   using E = typename S::elem;
   constexpr int u0p = gperm(MU, 0), u1p = gperm(MU, 1);
-  constexpr bool im = gimag(MU);
+  constexpr bool imag = gimag(MU);
   const float s = FWD ? -f : f;
   const uint32_t vh = (uint32_t)A.geo.vh;
   const uint32_t nrhs = (uint32_t)A.nrhs;
@@ -281,84 +293,147 @@ __device__ __forceinline__ void hop_pk(float2 (&acc)[4][N][R], const DslashArgs&
     for (int r = 0; r < R; r++) scale[r] = bc;
   }
 
-  float2 h[2][N][R], hs[2][N][R];  // hs = (h.y, h.x)
-  const uint32_t cs = vh * nrhs;
-  const uint32_t o = nb * nrhs + rhs0;
+  // projection (scalar FMAs, written straight into the lanes)
+  float2 hr[N][R], hi[N][R];
+  const uint32_t cs_bytes = vh * nrhs * (uint32_t)sizeof(E);
+  const char* base = reinterpret_cast<const char*>(in + (nb * nrhs + rhs0));
   const float k0 = s * (float)gsign(MU, 0), k1 = s * (float)gsign(MU, 1);
-  const float2 K0 = im ? make_float2(-k0, k0) : make_float2(k0, k0);
-  const float2 K1 = im ? make_float2(-k1, k1) : make_float2(k1, k1);
 #pragma unroll
   for (int a = 0; a < N; a++) {
     VecBuf<E, R> p0, p1, q0, q1;
-    Vec<E, R>::load(in + (o + (uint32_t)(0 * N + a) * cs), p0.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(1 * N + a) * cs), p1.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(u0p * N + a) * cs), q0.v);
-    Vec<E, R>::load(in + (o + (uint32_t)(u1p * N + a) * cs), q1.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(0 * N + a) * cs_bytes), p0.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(1 * N + a) * cs_bytes), p1.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u0p * N + a) * cs_bytes), q0.v);
+    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u1p * N + a) * cs_bytes), q1.v);
 #pragma unroll
     for (int r = 0; r < R; r++) {
       const float2 x0 = S::to_c(p0.v[r]), x1 = S::to_c(p1.v[r]);
       const float2 y0 = S::to_c(q0.v[r]), y1 = S::to_c(q1.v[r]);
-      if constexpr (im) {  // h = x + k i y = (x.x - k y.y, x.y + k y.x)
-        h[0][a][r] = __ffma2_rn(K0, make_float2(y0.y, y0.x), x0);
-        h[1][a][r] = __ffma2_rn(K1, make_float2(y1.y, y1.x), x1);
+      if constexpr (imag) {
+        hr[a][r].x = fmaf(-k0, y0.y, x0.x);
+        hi[a][r].x = fmaf(k0, y0.x, x0.y);
+        hr[a][r].y = fmaf(-k1, y1.y, x1.x);
+        hi[a][r].y = fmaf(k1, y1.x, x1.y);
       } else {
-        h[0][a][r] = __ffma2_rn(K0, y0, x0);
-        h[1][a][r] = __ffma2_rn(K1, y1, x1);
+        hr[a][r].x = fmaf(k0, y0.x, x0.x);
+        hi[a][r].x = fmaf(k0, y0.y, x0.y);
+        hr[a][r].y = fmaf(k1, y1.x, x1.x);
+        hi[a][r].y = fmaf(k1, y1.y, x1.y);
       }
-      hs[0][a][r] = make_float2(h[0][a][r].y, h[0][a][r].x);
-      hs[1][a][r] = make_float2(h[1][a][r].y, h[1][a][r].x);
     }
   }
 
+  const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
+  const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);
   const float klo0 = s * (float)gsign(MU, u0p), klo1 = s * (float)gsign(MU, u1p);
 #pragma unroll
   for (int a = 0; a < N; a++) {
-    float2 t[2][R];
+    float2 tr[R], ti[R];
 #pragma unroll
-    for (int u = 0; u < 2; u++)
-#pragma unroll
-      for (int r = 0; r < R; r++) t[u][r] = make_float2(0.f, 0.f);
+    for (int r = 0; r < R; r++) tr[r] = ti[r] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int b = 0; b < N; b++) {
       const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
-      const float2 uc = S::to_c(__ldg(gauge + (link_off + comp * vh)));
+      const float2 uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp * ls_bytes)));
       const float ui = FWD ? uc.y : -uc.y;
-      const float2 URR = make_float2(uc.x, uc.x), UII = make_float2(-ui, ui);
+      const float2 urr = make_float2(uc.x, uc.x), uii = make_float2(ui, ui), nuii = make_float2(-ui, -ui);
 #pragma unroll
-      for (int u = 0; u < 2; u++)
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-          t[u][r] = __ffma2_rn(URR, h[u][b][r], t[u][r]);
-          t[u][r] = __ffma2_rn(UII, hs[u][b][r], t[u][r]);
-        }
+      for (int r = 0; r < R; r++) {
+        tr[r] = __ffma2_rn(urr, hr[b][r], tr[r]);
+        tr[r] = __ffma2_rn(nuii, hi[b][r], tr[r]);
+        ti[r] = __ffma2_rn(urr, hi[b][r], ti[r]);
+        ti[r] = __ffma2_rn(uii, hr[b][r], ti[r]);
+      }
     }
 #pragma unroll
     for (int r = 0; r < R; r++) {
-      const float2 KU = make_float2(scale[r], scale[r]);
-      acc[0][a][r] = __ffma2_rn(KU, t[0][r], acc[0][a][r]);
-      acc[1][a][r] = __ffma2_rn(KU, t[1][r], acc[1][a][r]);
+      const float2 ku = make_float2(scale[r], scale[r]);
       const float kl0 = klo0 * scale[r], kl1 = klo1 * scale[r];
-      if constexpr (im) {  // acc += kl i t = (-kl t.y, kl t.x)
-        acc[u0p][a][r] = __ffma2_rn(make_float2(-kl0, kl0), make_float2(t[0][r].y, t[0][r].x), acc[u0p][a][r]);
-        acc[u1p][a][r] = __ffma2_rn(make_float2(-kl1, kl1), make_float2(t[1][r].y, t[1][r].x), acc[u1p][a][r]);
-      } else {
-        acc[u0p][a][r] = __ffma2_rn(make_float2(kl0, kl0), t[0][r], acc[u0p][a][r]);
-        acc[u1p][a][r] = __ffma2_rn(make_float2(kl1, kl1), t[1][r], acc[u1p][a][r]);
+      re[0][a][r] = __ffma2_rn(ku, tr[r], re[0][a][r]);
+      im[0][a][r] = __ffma2_rn(ku, ti[r], im[0][a][r]);
+      if constexpr (u0p == 2) {  // rows 2, 3 <- t rows 0, 1: lane-aligned
+        if constexpr (imag) {
+          re[1][a][r] = __ffma2_rn(make_float2(-kl0, -kl1), ti[r], re[1][a][r]);
+          im[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), tr[r], im[1][a][r]);
+        } else {
+          re[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), tr[r], re[1][a][r]);
+          im[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), ti[r], im[1][a][r]);
+        }
+      } else {  // rows 3, 2 <- t rows 0, 1: lanes crossed, scalar FMAs
+        if constexpr (imag) {
+          re[1][a][r].y = fmaf(-kl0, ti[r].x, re[1][a][r].y);
+          im[1][a][r].y = fmaf(kl0, tr[r].x, im[1][a][r].y);
+          re[1][a][r].x = fmaf(-kl1, ti[r].y, re[1][a][r].x);
+          im[1][a][r].x = fmaf(kl1, tr[r].y, im[1][a][r].x);
+        } else {
+          re[1][a][r].y = fmaf(kl0, tr[r].x, re[1][a][r].y);
+          im[1][a][r].y = fmaf(kl0, ti[r].x, im[1][a][r].y);
+          re[1][a][r].x = fmaf(kl1, tr[r].y, re[1][a][r].x);
+          im[1][a][r].x = fmaf(kl1, ti[r].y, im[1][a][r].x);
+        }
       }
     }
   }
 }
 
+// accumulator of one thread: complex rows, or the packed lane pairs of hop_pk
+template <typename T, int N, int R, bool PK>
+struct HopAcc {
+  C2<T> c[4][N][R];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int sp = 0; sp < 4; sp++)
+#pragma unroll
+      for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int r = 0; r < R; r++) c[sp][a][r].x = c[sp][a][r].y = (T)0;
+  }
+  __device__ __forceinline__ void to_rows(C2<T> (&acc)[4][N][R]) const {
+#pragma unroll
+    for (int sp = 0; sp < 4; sp++)
+#pragma unroll
+      for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[sp][a][r] = c[sp][a][r];
+  }
+};
+
+template <typename T, int N, int R>
+struct HopAcc<T, N, R, true> {
+  float2 re[2][N][R], im[2][N][R];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+      for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int r = 0; r < R; r++) re[s][a][r] = im[s][a][r] = make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ void to_rows(C2<T> (&acc)[4][N][R]) const {
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+#pragma unroll
+      for (int a = 0; a < N; a++)
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          acc[2 * s][a][r].x = re[s][a][r].x;
+          acc[2 * s][a][r].y = im[s][a][r].x;
+          acc[2 * s + 1][a][r].x = re[s][a][r].y;
+          acc[2 * s + 1][a][r].y = im[s][a][r].y;
+        }
+  }
+};
+
 template <int P, int N, int R, bool PK, int MU, bool FWD>
-__device__ __forceinline__ void hop_any(C2<typename Store<P>::real> (&acc)[4][N][R], const DslashArgs& A,
+__device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK>& acc, const DslashArgs& A,
                                        const typename Store<P>::elem* __restrict__ in,
                                        const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
                                        uint32_t nb, uint32_t rhs0, typename Store<P>::real bc,
                                        typename Store<P>::real f) {
   if constexpr (PK)
-    hop_pk<P, N, R, MU, FWD>(acc, A, in, gauge, link_off, nb, rhs0, bc, f);
+    hop_pk<P, N, R, MU, FWD>(acc.re, acc.im, A, in, gauge, link_off, nb, rhs0, bc, f);
   else
-    hop<P, N, R, MU, FWD>(acc, A, in, gauge, link_off, nb, rhs0, bc, f);
+    hop<P, N, R, MU, FWD>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
 }
 
 }  // namespace detail
@@ -401,13 +476,8 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
   const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
   constexpr uint32_t NN = N * N;
 
-  C2<T> acc[4][N][R];
-#pragma unroll
-  for (int sp = 0; sp < 4; sp++)
-#pragma unroll
-    for (int a = 0; a < N; a++)
-#pragma unroll
-      for (int r = 0; r < R; r++) acc[sp][a][r].x = acc[sp][a][r].y = (T)0;
+  HopAcc<T, N, R, PK> hacc;
+  hacc.zero();
 
   // link offsets: forward links at (mu, p, site), backward at (mu, 1-p, nb)
   const uint32_t lf = p * NN * vh + site;
@@ -416,21 +486,21 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
   {  // X
     const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
     const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-    hop_any<P, N, R, PK, 0, true>(acc, A, in, gauge, lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 0, false>(acc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, true>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Y
     const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
     const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
-    hop_any<P, N, R, PK, 1, true>(acc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 1, false>(acc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, true>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Z
     const uint32_t pl = A.geo.plane;
     const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
     const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
-    hop_any<P, N, R, PK, 2, true>(acc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 2, false>(acc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, true>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // T, with the optional antiperiodic sign
     const uint32_t cb = A.geo.cube;
@@ -439,18 +509,23 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
     const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
     const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
     const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
-    hop_any<P, N, R, PK, 3, true>(acc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
-    hop_any<P, N, R, PK, 3, false>(acc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
+    hop_any<P, N, R, PK, 3, true>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
+    hop_any<P, N, R, PK, 3, false>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
   }
 
-  // epilogue: out = a * acc + b * x
-  T ca, cbx;
+  C2<T> acc[4][N][R];
+  hacc.to_rows(acc);
+
+  // epilogue: out = a_r * acc + b * x, a_r per RHS when a_rhs is given
+  T ca[R], cbx;
   if constexpr (sizeof(T) == 4) {
-    ca = A.af;
     cbx = A.bf;
+#pragma unroll
+    for (int r = 0; r < R; r++) ca[r] = A.a_rhs_f ? A.a_rhs_f[rhs0 + r] : A.af;
   } else {
-    ca = (T)A.a;
     cbx = (T)A.b;
+#pragma unroll
+    for (int r = 0; r < R; r++) ca[r] = A.a_rhs_d ? (T)A.a_rhs_d[rhs0 + r] : (T)A.a;
   }
   const E* __restrict__ xin = static_cast<const E*>(A.x);
   float xs[R];
@@ -472,14 +547,14 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
           auto xc = S::to_c(xv.v[r]);
           T sx = cbx;
           if constexpr (S::has_norm) sx *= (T)xs[r];
-          acc[sp][a][r].x = fma(sx, (T)xc.x, ca * acc[sp][a][r].x);
-          acc[sp][a][r].y = fma(sx, (T)xc.y, ca * acc[sp][a][r].y);
+          acc[sp][a][r].x = fma(sx, (T)xc.x, ca[r] * acc[sp][a][r].x);
+          acc[sp][a][r].y = fma(sx, (T)xc.y, ca[r] * acc[sp][a][r].y);
         }
       } else {
 #pragma unroll
         for (int r = 0; r < R; r++) {
-          acc[sp][a][r].x *= ca;
-          acc[sp][a][r].y *= ca;
+          acc[sp][a][r].x *= ca[r];
+          acc[sp][a][r].y *= ca[r];
         }
       }
     }

@@ -43,7 +43,7 @@ __global__ void pack_fermions_kernel(PtrArray src, int mode, int parity, void* d
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
-  if ((int)site >= g.vh) return;
+  if ((int)site >= g.vh || src.p[r] == nullptr) return;  // a null pointer leaves RHS r untouched
   const double2* s = static_cast<const double2*>(src.p[r]) + src_site(mode, site, parity, g) * (4 * N);
   double2 v[4 * N];
 #pragma unroll
@@ -79,7 +79,7 @@ __global__ void unpack_fermions_kernel(PtrArray dstp, int mode, int parity, cons
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
-  if ((int)site >= g.vh) return;
+  if ((int)site >= g.vh || dstp.p[r] == nullptr) return;  // a null pointer skips RHS r
   const int64_t cs = (int64_t)g.vh * nrhs;
   const E* s = static_cast<const E*>(src) + (int64_t)site * nrhs + r;
   double2* d = static_cast<double2*>(const_cast<void*>(dstp.p[r])) + src_site(mode, site, parity, g) * (4 * N);
@@ -137,13 +137,13 @@ __global__ void unpack_gauge_kernel(const double2* __restrict__ src, double2* ds
 // convert an MRHS field between storage precisions (same layout)
 template <int PI, int PO>
 __global__ void convert_field_kernel(const void* src, const float* src_norm, void* dst, float* dst_norm,
-                                     int64_t vh, int ncomp, int nrhs, FastDiv div_nrhs) {
+                                     int64_t vh, int ncomp, int nrhs, FastDiv div_nrhs, const int* mask) {
   using SI = Store<PI>;
   using SO = Store<PO>;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
-  if ((int64_t)site >= vh) return;
+  if ((int64_t)site >= vh || (mask && !mask[r])) return;  // masked RHS keep their values
   // component-major: component c at (c * vh + site) * nrhs + r
   const int64_t cs = vh * nrhs;
   const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * nrhs + r;
@@ -297,17 +297,17 @@ void unpack_gauge_fp64(int N, const void* src, void* dst, const Geometry& g, cud
 }
 
 void convert_field(int prec_in, const void* src, const float* src_norm, int prec_out, void* dst, float* dst_norm,
-                   int64_t vh, int ncomp, int nrhs, cudaStream_t st) {
+                   int64_t vh, int ncomp, int nrhs, cudaStream_t st, const int* mask) {
   const int64_t threads = vh * nrhs;
   QCU_REQUIRE(threads < (1ll << 31), QCU_ERR_INVALID_ARGUMENT, "field too large");
   const int block = 256;
   const int grid = (int)((threads + block - 1) / block);
   FastDiv dn((uint32_t)nrhs);
-#define QCU_CONV(PI, PO)                                                                                       \
-  if (prec_in == PI && prec_out == PO) {                                                                       \
-    convert_field_kernel<PI, PO><<<grid, block, 0, st>>>(src, src_norm, dst, dst_norm, vh, ncomp, nrhs, dn);  \
-    QCU_CHECK_CUDA(cudaGetLastError());                                                                        \
-    return;                                                                                                    \
+#define QCU_CONV(PI, PO)                                                                                             \
+  if (prec_in == PI && prec_out == PO) {                                                                             \
+    convert_field_kernel<PI, PO><<<grid, block, 0, st>>>(src, src_norm, dst, dst_norm, vh, ncomp, nrhs, dn, mask);  \
+    QCU_CHECK_CUDA(cudaGetLastError());                                                                              \
+    return;                                                                                                          \
   }
   QCU_CONV(PREC_DOUBLE, PREC_SINGLE)
   QCU_CONV(PREC_DOUBLE, PREC_HALF)

@@ -30,9 +30,10 @@ void unpack_fermions(int prec, int N, const PtrArray& dst, int mode, int parity,
 void pack_gauge(int prec, int N, const void* src, int lex, void* dst, const Geometry& g, cudaStream_t st);
 // internal FP64 gauge -> caller eo layout
 void unpack_gauge_fp64(int N, const void* src, void* dst, const Geometry& g, cudaStream_t st);
-// MRHS field precision conversion (same [vh][ncomp][nrhs] layout)
+// MRHS field precision conversion (same [ncomp][vh][nrhs] layout); RHS whose
+// mask entry is 0 are left untouched (mask may be null)
 void convert_field(int prec_in, const void* src, const float* src_norm, int prec_out, void* dst, float* dst_norm,
-                   int64_t vh, int ncomp, int nrhs, cudaStream_t st);
+                   int64_t vh, int ncomp, int nrhs, cudaStream_t st, const int* mask = nullptr);
 // FP64 internal gauge -> the same layout in `prec` (no scales: |U_ab| <= 1)
 void convert_gauge(const void* src_fp64, int prec, void* dst, int64_t count, cudaStream_t st);
 // plain complex-double transpose [rows][cols] -> [cols][rows]

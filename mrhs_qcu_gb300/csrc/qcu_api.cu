@@ -15,6 +15,7 @@
 
 #include "../../include/qcu.h"
 #include "../../include/qcu_gb300.h"
+#include "serve.h"
 #include "session.h"
 
 using qcu::Error;
@@ -53,6 +54,28 @@ int guarded(F&& f) {
     record(QCU_ERR_OUT_OF_MEMORY, "host allocation failed");
     return QCU_ERR_OUT_OF_MEMORY;
   } catch (const std::exception& e) {
+    record(QCU_ERR_CUDA, e.what());
+    return QCU_ERR_CUDA;
+  }
+}
+
+// the same error handling without the global session lock (server calls,
+// which block or run concurrently with the session API)
+template <typename F>
+int guarded_unlocked(F&& f) {
+  try {
+    f();
+    return QCU_OK;
+  } catch (const Error& e) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    record(e.code, e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    record(QCU_ERR_OUT_OF_MEMORY, "host allocation failed");
+    return QCU_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    std::lock_guard<std::mutex> lk(g_mutex);
     record(QCU_ERR_CUDA, e.what());
     return QCU_ERR_CUDA;
   }
@@ -376,6 +399,27 @@ int qcuNorm2MRHS(double* out, const void* field, int precision, int nrhs) {
   });
 }
 
+int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, int* count) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    QCU_REQUIRE(count != nullptr && (shapes != nullptr || max_shapes == 0) && max_shapes >= 0,
+                QCU_ERR_INVALID_ARGUMENT, "qcuDslashKernels: bad output arrays");
+    int n = 0;
+    for (int R = 1; R <= 8; R++)
+      for (int pk = 0; pk < 2; pk++)
+        for (int m = 1; m <= 7; m++)
+          if (qcu::find_dslash(precision, nColors, R, m, pk)) {
+            if (n < max_shapes) {
+              shapes[3 * n] = R;
+              shapes[3 * n + 1] = m;
+              shapes[3 * n + 2] = pk;
+            }
+            n++;
+          }
+    *count = n;
+  });
+}
+
 int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed) {
   return guarded([&] {
     Session& s = session();
@@ -393,6 +437,8 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     A.x = nullptr;
     A.x_norm = nullptr;
     A.mask = nullptr;
+    A.a_rhs_f = nullptr;
+    A.a_rhs_d = nullptr;
     A.a = 1.0;
     A.b = 0.0;
     A.geo = s.geo;
@@ -406,6 +452,73 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (min_blocks) *min_blocks = c.minb;
     if (packed) *packed = c.pk;
   });
+}
+
+// ---- solve server ---------------------------------------------------------
+int qcuServerCreate(void** server, size_t hbm_budget_bytes, int max_slots_per_gauge, int inner_precision,
+                    int solver) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(server != nullptr, QCU_ERR_INVALID_ARGUMENT, "null server handle");
+    QCU_REQUIRE(solver == QCU_SOLVER_CG || solver == QCU_SOLVER_BICGSTAB, QCU_ERR_INVALID_ARGUMENT, "bad solver");
+    *server = new qcu::Server(hbm_budget_bytes, max_slots_per_gauge, inner_precision, solver);
+  });
+}
+
+int qcuServerAddGauge(void* server, int gauge_id, const int lattice[4], int nColors, const void* gauge,
+                      int antiperiodic_t) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(server && lattice && gauge, QCU_ERR_INVALID_ARGUMENT, "null argument");
+    QcuParam p;
+    for (int i = 0; i < 4; i++) p.lattice_size[i] = lattice[i];
+    check_lattice(&p);
+    QCU_REQUIRE(nColors >= 3 && nColors <= 8, QCU_ERR_UNSUPPORTED, "nColors must be in 3..8");
+    static_cast<qcu::Server*>(server)->add_gauge(gauge_id, lattice, nColors, gauge, antiperiodic_t);
+  });
+}
+
+int qcuServerSubmit(void* server, int gauge_id, double kappa, double tol, int nrhs, void* const* x,
+                    void* const* b, long long* request_id) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(server && request_id, QCU_ERR_INVALID_ARGUMENT, "null argument");
+    *request_id = static_cast<qcu::Server*>(server)->submit(gauge_id, kappa, tol, nrhs, x, b);
+  });
+}
+
+int qcuServerWait(void* server, long long request_id, double timeout_s, QcuRequestInfo* info) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(server != nullptr, QCU_ERR_INVALID_ARGUMENT, "null server");
+    qcu::RequestInfo ri;
+    static_cast<qcu::Server*>(server)->wait(request_id, timeout_s, &ri);
+    if (info) {
+      info->done = ri.done;
+      info->status = ri.status;
+      info->nrhs = ri.nrhs;
+      info->iterations = ri.iterations;
+      info->latency_s = ri.latency_s;
+      info->queue_s = ri.queue_s;
+      info->max_true_residual = ri.max_true_residual;
+      info->all_converged = ri.all_converged;
+    }
+  });
+}
+
+int qcuServerStats(void* server, QcuServerStats* stats) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(server && stats, QCU_ERR_INVALID_ARGUMENT, "null argument");
+    qcu::ServerStats s = static_cast<qcu::Server*>(server)->stats();
+    stats->submitted = s.submitted;
+    stats->completed = s.completed;
+    stats->p50_s = s.p50_s;
+    stats->p99_s = s.p99_s;
+    stats->mean_s = s.mean_s;
+    stats->solves_per_s = s.solves_per_s;
+    stats->rhs_per_s = s.rhs_per_s;
+    stats->hbm_used = s.hbm_used;
+  });
+}
+
+int qcuServerDestroy(void* server) {
+  return guarded_unlocked([&] { delete static_cast<qcu::Server*>(server); });
 }
 
 void qcuSolverParamDefaults(QcuSolverParam* p) {

@@ -191,7 +191,9 @@ Session::~Session() {
 
 cudaStream_t Session::stream() {
   if (user_stream_) return user_stream_;
-  if (!own_stream_) QCU_CHECK_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamDefault));
+  if (!own_stream_)
+    QCU_CHECK_CUDA(
+        cudaStreamCreateWithFlags(&own_stream_, nonblocking_stream ? cudaStreamNonBlocking : cudaStreamDefault));
   return own_stream_;
 }
 
@@ -230,7 +232,7 @@ FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {
 }
 
 void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagger, double a, double b,
-                  const int* mask) {
+                  const int* mask, const float* a_rhs_f, const double* a_rhs_d) {
   QCU_REQUIRE(parity == 0 || parity == 1, QCU_ERR_INVALID_ARGUMENT, "parity must be 0 or 1");
   QCU_REQUIRE(dagger == 0 || dagger == 1, QCU_ERR_INVALID_ARGUMENT, "daggerFlag must be 0 or 1");
   QCU_REQUIRE(out.prec == in.prec && (!x.data || x.prec == in.prec), QCU_ERR_INVALID_ARGUMENT,
@@ -246,6 +248,8 @@ void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagg
   A.x = x.data;
   A.x_norm = x.norm;
   A.mask = mask;
+  A.a_rhs_f = a_rhs_f;
+  A.a_rhs_d = a_rhs_d;
   A.a = a;
   A.b = b;
   A.geo = geo;

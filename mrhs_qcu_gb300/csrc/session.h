@@ -133,6 +133,12 @@ class Session {
   Workspace ws;
   Autotuner& tuner;
 
+  // The library's own stream is a blocking stream (ordered after work on the
+  // legacy default stream, as a caller of the drop-in ABI expects) unless
+  // nonblocking_stream is set before its first use: the solve server's lanes
+  // capture CUDA graphs on worker threads, and a capture on a blocking stream
+  // makes every legacy-stream call of other threads fail meanwhile.
+  bool nonblocking_stream = false;
   cudaStream_t stream();
   void set_user_stream(cudaStream_t s) { user_stream_ = s; }
   void sync();
@@ -148,9 +154,11 @@ class Session {
   size_t norm_bytes(int prec, int nrhs) const { return prec_is16(prec) ? (size_t)geo.vh * nrhs * 4 : 0; }
   FieldView alloc_field(const std::string& name, int prec, int nrhs);
 
-  // out = a * D in + b * x  (x.data may be null), on the library stream
+  // out = a * D in + b * x  (x.data may be null), on the library stream.
+  // mask: per-RHS activity (masked RHS are left untouched); a_rhs_f / a_rhs_d:
+  // per-RHS a (device arrays) for FP32 / FP64 arithmetic, replacing a.
   void hop(FieldView out, FieldView in, FieldView x, int parity, int dagger, double a, double b,
-           const int* mask = nullptr);
+           const int* mask = nullptr, const float* a_rhs_f = nullptr, const double* a_rhs_d = nullptr);
 
   Blas& blas();
   double* scalars(size_t count);  // device scratch for per-RHS scalars

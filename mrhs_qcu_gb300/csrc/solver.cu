@@ -3,9 +3,9 @@
 // empty stub (src/qcu.cu:173 of the reference); this is new work built on the
 // MRHS hopping kernel.
 //
-// Schur system on the even sites:
-//   Mhat = 1 - kappa^2 D_eo D_oe,   bhat = b_e + kappa D_eo b_o,
-//   x_o  = b_o + kappa D_oe x_e,
+// Schur system on the even sites, per RHS r with its own kappa_r:
+//   Mhat_r = 1 - kappa_r^2 D_eo D_oe,   bhat_r = b_e + kappa_r D_eo b_o,
+//   x_o    = b_o + kappa_r D_oe x_e,
 // and Mhat^dag = 1 - kappa^2 D_eo^- D_oe^- (the dagger flag f = -1), because
 // D^dag = gamma5 D gamma5 is the hop with f = -1.  With x_o reconstructed
 // that way, |b - M x| over the full lattice equals |bhat - Mhat x_e|.
@@ -19,14 +19,20 @@
 // FP16 or BF16 storage).  FP64 is used for exactly three things: the solution
 // accumulator x, the true residual bhat - Mhat x recomputed at each reliable
 // update, and every inner product / norm (FP64 accumulation in the BLAS
-// reductions).  A reliable update happens when the iterated |s| of any RHS
-// drops below delta times its value at the previous update, or when it
-// reaches the tolerance.
+// reductions).
 //
-// Per-RHS scalars (alpha, beta, omega, ...) and the activity mask stay on the
-// device; a converged RHS is masked out of the hopping kernels and gets zero
-// coefficients, so chunks of iterations run without host round trips and can
-// be captured as CUDA graphs.
+// Slots.  The engine owns `capacity` RHS slots.  A slot is admitted (its
+// source packed, its state initialised), iterates, and is retired (its
+// solution unpacked) independently of the others: every per-RHS scalar
+// (alpha, beta, kappa, tolerance, ...) and the activity mask live in device
+// arrays, and every per-slot initialisation / update is a masked operation.
+// Reliable updates are per slot too: slot r is updated when its own iterated
+// residual has dropped by delta since its last update or reached its
+// tolerance.  A slot's arithmetic therefore depends only on its own data and
+// iteration count, not on which other slots are occupied.  Iterations run in
+// chunks of 8 with no host round trip; a chunk is captured once as a CUDA
+// graph and replayed.  Between chunks the host retires finished slots and
+// admits new ones (continuous batching, used by the serving loop).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -34,36 +40,14 @@
 #include <cstdlib>
 #include <cstring>
 
-#include "session.h"
+#include "solver.h"
 
 namespace qcu {
 namespace {
 
 constexpr int kChunk = 8;  // iterations between host checks
 
-struct Scalars {
-  double* rr;
-  double* rr_new;
-  double* qq;
-  double* ss;
-  double* ss_true;
-  double* maxss;
-  double* stop2;
-  double* bb;
-  double2* alpha;
-  double2* nalpha;
-  double2* beta;
-  double2* omega;
-  double2* nomega;
-  double2* rho;
-  double2* tmp1;
-  double2* tmp2;
-  double2* nbo;  // -beta * omega
-  int* active;
-  int* status;  // [0] active count, [1] update requested, [2] breakdown
-};
-
-__global__ void cg_alpha_kernel(Scalars S, int nrhs) {
+__global__ void cg_alpha_kernel(SolverScalars S, int nrhs) {
   const int r = threadIdx.x;
   if (r >= nrhs) return;
   double a = 0.0;
@@ -73,17 +57,17 @@ __global__ void cg_alpha_kernel(Scalars S, int nrhs) {
       a = S.rr[r] / q;
     } else {
       S.active[r] = 0;
-      S.status[2] = 1;
+      S.upd[r] = 1;
     }
   }
   S.alpha[r] = make_double2(a, 0.0);
   S.nalpha[r] = make_double2(-a, 0.0);
 }
 
-// beta, convergence and reliable-update test; one block of >= nrhs threads
-__global__ void cg_beta_kernel(Scalars S, int nrhs, double delta2) {
+// beta, convergence and reliable-update test per slot; one block of >= nrhs threads
+__global__ void cg_beta_kernel(SolverScalars S, int nrhs, double delta2) {
   const int r = threadIdx.x;
-  int act = 0, upd = 0;
+  int act = 0;
   if (r < nrhs) {
     double b = 0.0;
     if (S.active[r]) {
@@ -92,37 +76,20 @@ __global__ void cg_beta_kernel(Scalars S, int nrhs, double delta2) {
       const double ss = S.ss[r];
       if (!(ss > S.stop2[r])) {  // reached the tolerance (or NaN): verify in FP64
         S.active[r] = 0;
-        upd = 1;
+        S.upd[r] = 1;
       } else if (ss < delta2 * S.maxss[r]) {
-        upd = 1;
+        S.upd[r] = 1;
       }
       act = S.active[r];
     }
     S.beta[r] = make_double2(b, 0.0);
   }
   const int n_act = __syncthreads_count(act);
-  const int n_upd = __syncthreads_count(upd);
-  if (threadIdx.x == 0) {
-    S.status[0] = n_act;
-    if (n_upd) S.status[1] = 1;
-  }
-}
-
-// After a reliable update replaces r by the recomputed residual, restore the
-// CG invariant <r, p> = |r|^2 by p <- p + c r, c = 1 - <r, p> / |r|^2 (tmp1 =
-// <r, p>).  With a 16-bit operator the iterated residual drifts away from the
-// true one between updates; keeping p unchanged then breaks conjugacy.
-__global__ void cg_restore_kernel(Scalars S, int nrhs) {
-  const int r = threadIdx.x;
-  if (r >= nrhs) return;
-  double2 c = make_double2(0.0, 0.0);
-  const double rr = S.rr[r];
-  if (S.active[r] && rr > 0.0 && isfinite(rr)) c = make_double2(1.0 - S.tmp1[r].x / rr, -S.tmp1[r].y / rr);
-  S.tmp2[r] = c;
+  if (threadIdx.x == 0) S.status[0] = n_act;
 }
 
 // BiCGStab: alpha = rho / <r0, v>
-__global__ void bicg_alpha_kernel(Scalars S, int nrhs) {
+__global__ void bicg_alpha_kernel(SolverScalars S, int nrhs) {
   const int r = threadIdx.x;
   if (r >= nrhs) return;
   double2 a = make_double2(0.0, 0.0);
@@ -133,7 +100,7 @@ __global__ void bicg_alpha_kernel(Scalars S, int nrhs) {
       a = make_double2((rho.x * d.x + rho.y * d.y) / den, (rho.y * d.x - rho.x * d.y) / den);
     } else {
       S.active[r] = 0;
-      S.status[2] = 1;
+      S.upd[r] = 1;
     }
   }
   S.alpha[r] = a;
@@ -141,7 +108,7 @@ __global__ void bicg_alpha_kernel(Scalars S, int nrhs) {
 }
 
 // omega = <t, s> / <t, t>   (tmp1 = <t, s>, qq = |t|^2)
-__global__ void bicg_omega_kernel(Scalars S, int nrhs) {
+__global__ void bicg_omega_kernel(SolverScalars S, int nrhs) {
   const int r = threadIdx.x;
   if (r >= nrhs) return;
   double2 w = make_double2(0.0, 0.0);
@@ -151,7 +118,7 @@ __global__ void bicg_omega_kernel(Scalars S, int nrhs) {
       w = make_double2(S.tmp1[r].x / tt, S.tmp1[r].y / tt);
     } else {
       S.active[r] = 0;
-      S.status[2] = 1;
+      S.upd[r] = 1;
     }
   }
   S.omega[r] = w;
@@ -159,14 +126,13 @@ __global__ void bicg_omega_kernel(Scalars S, int nrhs) {
 }
 
 // beta = (rho_new / rho) (alpha / omega); tmp2 = rho_new; test |r|
-__global__ void bicg_beta_kernel(Scalars S, int nrhs, double delta2) {
+__global__ void bicg_beta_kernel(SolverScalars S, int nrhs, double delta2) {
   const int r = threadIdx.x;
-  int act = 0, upd = 0;
+  int act = 0;
   if (r < nrhs) {
     double2 b = make_double2(0.0, 0.0), nbo = make_double2(0.0, 0.0);
     if (S.active[r]) {
       const double2 rn = S.tmp2[r], ro = S.rho[r], a = S.alpha[r], w = S.omega[r];
-      // q1 = rn / ro, q2 = a / w
       const double d1 = ro.x * ro.x + ro.y * ro.y, d2 = w.x * w.x + w.y * w.y;
       if (d1 > 0.0 && d2 > 0.0 && isfinite(d1) && isfinite(d2)) {
         const double2 q1 = make_double2((rn.x * ro.x + rn.y * ro.y) / d1, (rn.y * ro.x - rn.x * ro.y) / d1);
@@ -176,15 +142,15 @@ __global__ void bicg_beta_kernel(Scalars S, int nrhs, double delta2) {
         S.rho[r] = rn;
       } else {
         S.active[r] = 0;
-        S.status[2] = 1;
+        S.upd[r] = 1;
       }
       const double ss = S.ss[r];
       if (S.active[r]) {
         if (!(ss > S.stop2[r])) {
           S.active[r] = 0;
-          upd = 1;
+          S.upd[r] = 1;
         } else if (ss < delta2 * S.maxss[r]) {
-          upd = 1;
+          S.upd[r] = 1;
         }
       }
       act = S.active[r];
@@ -193,361 +159,470 @@ __global__ void bicg_beta_kernel(Scalars S, int nrhs, double delta2) {
     S.nbo[r] = nbo;
   }
   const int n_act = __syncthreads_count(act);
-  const int n_upd = __syncthreads_count(upd);
-  if (threadIdx.x == 0) {
-    S.status[0] = n_act;
-    if (n_upd) S.status[1] = 1;
-  }
+  if (threadIdx.x == 0) S.status[0] = n_act;
 }
 
-FieldRef ref(const FieldView& f, const Session& s) {
+// masked-operation coefficients from sel: cm = sel, ck = 1 - sel, cn = -sel
+__global__ void select_coeffs_kernel(SolverScalars S, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs) return;
+  const double m = S.sel[r] ? 1.0 : 0.0;
+  S.cm[r] = make_double2(m, 0.0);
+  S.ck[r] = make_double2(1.0 - m, 0.0);
+  S.cn[r] = make_double2(-m, 0.0);
+  S.zero[r] = make_double2(0.0, 0.0);
+  S.one[r] = make_double2(1.0, 0.0);
+}
+
+// after a (re)start of the selected slots: rr, maxss and ss from the fresh
+// residuals; the CG invariant <r, p> = |r|^2 restored by p += c r with
+// c = 1 - <r, p> / |r|^2 (fresh slots have p = 0, so p becomes r).  The
+// update p += c r runs over every slot, so c = 0 for the slots not restarted.
+__global__ void restart_kernel(SolverScalars S, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs) return;
+  if (!S.sel[r]) {
+    S.tmp2[r] = make_double2(0.0, 0.0);
+    return;
+  }
+  S.rr[r] = S.rr_new[r];
+  S.maxss[r] = S.ss_true[r];
+  S.ss[r] = S.ss_true[r];
+  S.upd[r] = 0;
+  const double rr = S.rr_new[r];
+  double2 c = make_double2(0.0, 0.0);
+  if (rr > 0.0 && isfinite(rr)) c = make_double2(1.0 - S.tmp1[r].x / rr, -S.tmp1[r].y / rr);
+  S.tmp2[r] = c;
+}
+
+// BiCGStab restart of the selected slots: rho = <r0, r> (tmp1)
+__global__ void bicg_restart_kernel(SolverScalars S, int nrhs) {
+  const int r = threadIdx.x;
+  if (r >= nrhs || !S.sel[r]) return;
+  S.maxss[r] = S.ss_true[r];
+  S.ss[r] = S.ss_true[r];
+  S.upd[r] = 0;
+  S.rho[r] = S.tmp1[r];
+}
+
+}  // namespace
+
+FieldRef SlotEngine::ref(const FieldView& f) const {
   FieldRef r;
   r.data = f.data;
   r.prec = f.prec;
   r.nrhs = f.nrhs;
-  r.n = (int64_t)s.geo.vh * 4 * s.N * f.nrhs;
+  r.n = (int64_t)s_.geo.vh * 4 * s_.N * f.nrhs;
   return r;
 }
 
-class Solver {
- public:
-  Solver(Session& s, int nrhs, const SolveRequest& q) : s_(s), n_(nrhs), q_(q) {
-    kp_ = q.inner_prec == PREC_DOUBLE ? PREC_DOUBLE : PREC_SINGLE;
-    op_ = q.inner_prec;
-    kappa2_ = q.kappa * q.kappa;
-    delta2_ = (q.inner_prec == PREC_DOUBLE) ? 0.0 : q.delta * q.delta;
-    st_ = s.stream();
-    // FP64 fields
-    be_ = s.alloc_field("sv.be", PREC_DOUBLE, n_);
-    bo_ = s.alloc_field("sv.bo", PREC_DOUBLE, n_);
-    bh_ = s.alloc_field("sv.bh", PREC_DOUBLE, n_);
-    xh_ = s.alloc_field("sv.xh", PREC_DOUBLE, n_);
-    xo_ = s.alloc_field("sv.xo", PREC_DOUBLE, n_);
-    sh_ = s.alloc_field("sv.sh", PREC_DOUBLE, n_);
-    th_ = s.alloc_field("sv.th", PREC_DOUBLE, n_);
-    tmp64_ = s.alloc_field("sv.tmp64", PREC_DOUBLE, n_);
-    // Krylov fields
-    xl_ = s.alloc_field("sv.xl", kp_, n_);
-    sl_ = s.alloc_field("sv.sl", kp_, n_);
-    rl_ = s.alloc_field("sv.rl", kp_, n_);
-    pl_ = s.alloc_field("sv.pl", kp_, n_);
-    ql_ = s.alloc_field("sv.ql", kp_, n_);
-    wl_ = s.alloc_field("sv.wl", kp_, n_);
-    r0l_ = s.alloc_field("sv.r0l", kp_, n_);
-    // operator-precision fields
-    if (op_ != kp_) {
-      pop_ = s.alloc_field("sv.pop", op_, n_);
-      qop_ = s.alloc_field("sv.qop", op_, n_);
-      wop_ = s.alloc_field("sv.wop", op_, n_);
-    }
-    tmpop_ = s.alloc_field("sv.tmpop", op_, n_);
-    // scalars
-    const int R = QCU_MAX_RHS;
-    double* d = s.scalars((size_t)R * 40 + 16);
-    S_.rr = d;
-    S_.rr_new = d + R;
-    S_.qq = d + 2 * R;
-    S_.ss = d + 3 * R;
-    S_.ss_true = d + 4 * R;
-    S_.maxss = d + 5 * R;
-    S_.stop2 = d + 6 * R;
-    S_.bb = d + 7 * R;
-    double2* c = reinterpret_cast<double2*>(d + 8 * R);
-    S_.alpha = c;
-    S_.nalpha = c + R;
-    S_.beta = c + 2 * R;
-    S_.omega = c + 3 * R;
-    S_.nomega = c + 4 * R;
-    S_.rho = c + 5 * R;
-    S_.tmp1 = c + 6 * R;
-    S_.tmp2 = c + 7 * R;
-    S_.nbo = c + 8 * R;
-    int* ip = reinterpret_cast<int*>(c + 9 * R);  // d + 26R ..
-    S_.active = ip;
-    S_.status = ip + R;
-    ones_ = reinterpret_cast<double2*>(s.ws.get("sv.ones", sizeof(double2) * R));
-    mones_ = reinterpret_cast<double2*>(s.ws.get("sv.mones", sizeof(double2) * R));
-    kap_ = reinterpret_cast<double2*>(s.ws.get("sv.kap", sizeof(double2) * R));
-    std::vector<double2> h(R);
-    for (auto& v : h) v = make_double2(1.0, 0.0);
-    QCU_CHECK_CUDA(cudaMemcpyAsync(ones_, h.data(), sizeof(double2) * R, cudaMemcpyHostToDevice, st_));
-    for (auto& v : h) v = make_double2(-1.0, 0.0);
-    QCU_CHECK_CUDA(cudaMemcpyAsync(mones_, h.data(), sizeof(double2) * R, cudaMemcpyHostToDevice, st_));
-    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+size_t SlotEngine::bytes_needed(const Session& s, int capacity, int inner_prec) {
+  const int kp = inner_prec == PREC_DOUBLE ? PREC_DOUBLE : PREC_SINGLE;
+  size_t b = 8 * s.field_bytes(PREC_DOUBLE, capacity) + 7 * s.field_bytes(kp, capacity);
+  if (inner_prec != kp) b += 3 * (s.field_bytes(inner_prec, capacity) + s.norm_bytes(inner_prec, capacity));
+  b += s.field_bytes(inner_prec, capacity) + s.norm_bytes(inner_prec, capacity);
+  return b;
+}
+
+SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const std::string& tag)
+    : s_(s), n_(capacity), q_(q) {
+  QCU_REQUIRE(capacity >= 1 && capacity <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "slot capacity must be in 1..256");
+  QCU_REQUIRE(q.solver == 0 || q.solver == 1, QCU_ERR_INVALID_ARGUMENT, "unknown solver");
+  QCU_REQUIRE(prec_valid(q.inner_prec), QCU_ERR_INVALID_ARGUMENT, "bad inner precision");
+  kp_ = q.inner_prec == PREC_DOUBLE ? PREC_DOUBLE : PREC_SINGLE;
+  op_ = q.inner_prec;
+  delta2_ = (q.inner_prec == PREC_DOUBLE) ? 0.0 : q.delta * q.delta;
+  st_ = s.stream();
+  const std::string t = tag + ".";
+  be_ = s.alloc_field(t + "be", PREC_DOUBLE, n_);
+  bo_ = s.alloc_field(t + "bo", PREC_DOUBLE, n_);
+  bh_ = s.alloc_field(t + "bh", PREC_DOUBLE, n_);
+  xh_ = s.alloc_field(t + "xh", PREC_DOUBLE, n_);
+  xo_ = s.alloc_field(t + "xo", PREC_DOUBLE, n_);
+  sh_ = s.alloc_field(t + "sh", PREC_DOUBLE, n_);
+  th_ = s.alloc_field(t + "th", PREC_DOUBLE, n_);
+  tmp64_ = s.alloc_field(t + "tmp64", PREC_DOUBLE, n_);
+  xl_ = s.alloc_field(t + "xl", kp_, n_);
+  sl_ = s.alloc_field(t + "sl", kp_, n_);
+  rl_ = s.alloc_field(t + "rl", kp_, n_);
+  pl_ = s.alloc_field(t + "pl", kp_, n_);
+  ql_ = s.alloc_field(t + "ql", kp_, n_);
+  wl_ = s.alloc_field(t + "wl", kp_, n_);
+  r0l_ = s.alloc_field(t + "r0l", kp_, n_);
+  if (op_ != kp_) {
+    pop_ = s.alloc_field(t + "pop", op_, n_);
+    qop_ = s.alloc_field(t + "qop", op_, n_);
+    wop_ = s.alloc_field(t + "wop", op_, n_);
   }
-
-  ~Solver() {
-    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+  tmpop_ = s.alloc_field(t + "tmpop", op_, n_);
+  // per-slot device scalars
+  const int R = QCU_MAX_RHS;
+  char* d = static_cast<char*>(s.ws.get(t + "scalars", (size_t)R * 64 * sizeof(double) + 4096));
+  double* dd = reinterpret_cast<double*>(d);
+  S_.rr = dd;
+  S_.rr_new = dd + R;
+  S_.qq = dd + 2 * R;
+  S_.ss = dd + 3 * R;
+  S_.ss_true = dd + 4 * R;
+  S_.maxss = dd + 5 * R;
+  S_.stop2 = dd + 6 * R;
+  S_.bb = dd + 7 * R;
+  S_.bo2 = dd + 8 * R;
+  S_.kap_d = dd + 9 * R;
+  S_.nk2_d = dd + 10 * R;
+  double2* c = reinterpret_cast<double2*>(dd + 11 * R);
+  S_.alpha = c;
+  S_.nalpha = c + R;
+  S_.beta = c + 2 * R;
+  S_.omega = c + 3 * R;
+  S_.nomega = c + 4 * R;
+  S_.rho = c + 5 * R;
+  S_.tmp1 = c + 6 * R;
+  S_.tmp2 = c + 7 * R;
+  S_.nbo = c + 8 * R;
+  S_.cm = c + 9 * R;
+  S_.ck = c + 10 * R;
+  S_.cn = c + 11 * R;
+  S_.zero = c + 12 * R;
+  S_.one = c + 13 * R;
+  float* ff = reinterpret_cast<float*>(c + 14 * R);  // at dd + 39R
+  S_.nk2_f = ff;
+  int* ip = reinterpret_cast<int*>(ff + R);
+  S_.active = ip;
+  S_.upd = ip + R;
+  S_.sel = ip + 2 * R;
+  S_.status = ip + 3 * R;
+  host_.assign(n_, SlotState{});
+  QCU_CHECK_CUDA(cudaMemsetAsync(d, 0, (size_t)R * 64 * sizeof(double) + 4096, st_));
+  // every field starts at zero: masked slots never meet uninitialised memory
+  for (FieldView* f : {&be_, &bo_, &bh_, &xh_, &xo_, &sh_, &th_, &tmp64_, &xl_, &sl_, &rl_, &pl_, &ql_, &wl_, &r0l_,
+                       &pop_, &qop_, &wop_, &tmpop_}) {
+    if (!f->data) continue;
+    QCU_CHECK_CUDA(cudaMemsetAsync(f->data, 0, s.field_bytes(f->prec, n_), st_));
+    if (f->norm) QCU_CHECK_CUDA(cudaMemsetAsync(f->norm, 0, s.norm_bytes(f->prec, n_), st_));
   }
+  s.blas();  // BLAS scratch, before any graph capture
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+}
 
-  SolveResult run(void* const* x, void* const* b) {
-    auto t0 = std::chrono::steady_clock::now();
-    SolveResult res;
-    Blas& B = s_.blas();
-    PtrArray pb{}, px{};
-    for (int r = 0; r < n_; r++) {
-      pb.p[r] = b[r];
-      px.p[r] = x[r];
-    }
-    // zero every work field so masked RHS never meet uninitialised memory
-    for (FieldView* f : {&xh_, &xo_, &sh_, &th_, &tmp64_, &xl_, &sl_, &rl_, &pl_, &ql_, &wl_, &r0l_, &pop_, &qop_,
-                         &wop_, &tmpop_}) {
-      if (!f->data) continue;
-      QCU_CHECK_CUDA(cudaMemsetAsync(f->data, 0, s_.field_bytes(f->prec, n_), st_));
-      if (f->norm) QCU_CHECK_CUDA(cudaMemsetAsync(f->norm, 0, s_.norm_bytes(f->prec, n_), st_));
-    }
-    pack_fermions(PREC_DOUBLE, s_.N, pb, q_.src_mode, 0, be_.data, nullptr, s_.geo, n_, st_);
-    pack_fermions(PREC_DOUBLE, s_.N, pb, q_.src_mode, 1, bo_.data, nullptr, s_.geo, n_, st_);
-    // |b|^2 over both parities; stop when |s|^2 <= tol^2 |b|^2
-    B.norm2(ref(be_, s_), S_.bb, st_);
-    B.norm2(ref(bo_, s_), S_.ss_true, st_);
-    std::vector<double> bb(n_), bo2(n_);
-    QCU_CHECK_CUDA(cudaMemcpyAsync(bb.data(), S_.bb, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(bo2.data(), S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-    stop2_host_.resize(n_);
-    bb_host_.resize(n_);
-    for (int r = 0; r < n_; r++) {
-      bb_host_[r] = bb[r] + bo2[r];
-      stop2_host_[r] = q_.tol * q_.tol * bb_host_[r];
-    }
-    QCU_CHECK_CUDA(cudaMemcpyAsync(S_.stop2, stop2_host_.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, st_));
-    // bhat = b_e + kappa D_eo b_o
-    s_.hop(bh_, bo_, be_, 0, 0, q_.kappa, 1.0);
+SlotEngine::~SlotEngine() {
+  if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+}
 
-    converged_.assign(n_, 0);
-    std::vector<int> zero_act(n_, 0);
-    int iters = 0;
-    bool any_active = reliable_update(true);
-    res.reliable_updates = 0;
-    if (q_.solver == 0) {
-      B.copy(ref(rl_, s_), ref(pl_, s_), st_);
-    } else {
-      B.copy(ref(sl_, s_), ref(r0l_, s_), st_);  // shadow residual
-      B.copy(ref(sl_, s_), ref(pl_, s_), st_);
-      B.cdot(ref(r0l_, s_), ref(sl_, s_), S_.rho, st_);
-    }
-    while (any_active && iters < q_.max_iter) {
-      const int k = std::min(chunk_, q_.max_iter - iters);
-      run_chunk(k);
-      iters += k;
-      int status[3];
-      QCU_CHECK_CUDA(cudaMemcpyAsync(status, S_.status, sizeof(int) * 3, cudaMemcpyDeviceToHost, st_));
-      QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-      if (verbose_) trace(iters, status);
-      if (status[1] || status[0] == 0 || status[2]) {
-        any_active = reliable_update(false);
-        res.reliable_updates++;
-        if (any_active && q_.solver == 1) {
-          // restart the BiCGStab recurrence from the corrected residual
-          B.copy(ref(sl_, s_), ref(pl_, s_), st_);
-          B.cdot(ref(r0l_, s_), ref(sl_, s_), S_.rho, st_);
-        }
+std::vector<int> SlotEngine::free_slots() const {
+  std::vector<int> f;
+  for (int r = 0; r < n_; r++)
+    if (host_[r].phase == SlotState::FREE) f.push_back(r);
+  return f;
+}
+
+int SlotEngine::active_slots() const {
+  int k = 0;
+  for (int r = 0; r < n_; r++) k += host_[r].phase == SlotState::ACTIVE;
+  return k;
+}
+
+void SlotEngine::upload_sel(const std::vector<int>& slots) {
+  std::vector<int> m(n_, 0);
+  for (int r : slots) m[r] = 1;
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.sel, m.data(), sizeof(int) * n_, cudaMemcpyHostToDevice, st_));
+  select_coeffs_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+  QCU_CHECK_CUDA(cudaGetLastError());
+  // the upload reads host memory asynchronously: keep it alive until done
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+}
+
+void SlotEngine::upload_kappa() {
+  std::vector<double> k(n_), nk2(n_);
+  std::vector<float> nk2f(n_);
+  for (int r = 0; r < n_; r++) {
+    k[r] = host_[r].kappa;
+    nk2[r] = -host_[r].kappa * host_[r].kappa;
+    nk2f[r] = (float)nk2[r];
+  }
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.kap_d, k.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.nk2_d, nk2.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.nk2_f, nk2f.data(), sizeof(float) * n_, cudaMemcpyHostToDevice, st_));
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+}
+
+// out = Mhat in (dagger 0) or Mhat^dag in (dagger 1) for the slots in mask,
+// fields in precision `prec` with per-slot kappa
+void SlotEngine::apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, int dagger,
+                            const int* mask) {
+  s_.hop(tmp, in, FieldView{}, 1, dagger, 1.0, 0.0, mask);
+  if (in.prec == PREC_DOUBLE)
+    s_.hop(out, tmp, in, 0, dagger, 0.0, 1.0, mask, nullptr, S_.nk2_d);
+  else
+    s_.hop(out, tmp, in, 0, dagger, 0.0, 1.0, mask, S_.nk2_f, nullptr);
+}
+
+// Krylov-precision out = Mhat in (or Mhat^dag) for the slots in mask
+void SlotEngine::op_apply(const FieldView& out_kp, const FieldView& in_kp, int dagger, const int* mask) {
+  if (op_ == kp_) {
+    apply_mhat(out_kp, in_kp, tmpop_, dagger, mask);
+  } else {
+    convert_field(kp_, in_kp.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_, mask);
+    apply_mhat(qop_, pop_, tmpop_, dagger, mask);
+    convert_field(op_, qop_.data, qop_.norm, kp_, out_kp.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, mask);
+  }
+}
+
+void SlotEngine::cg_iteration() {
+  Blas& B = s_.blas();
+  if (op_ == kp_) {
+    apply_mhat(ql_, pl_, tmpop_, 0, S_.active);
+    apply_mhat(wl_, ql_, tmpop_, 1, S_.active);
+  } else {
+    convert_field(kp_, pl_.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
+    apply_mhat(qop_, pop_, tmpop_, 0, S_.active);
+    apply_mhat(wop_, qop_, tmpop_, 1, S_.active);
+    convert_field(op_, qop_.data, qop_.norm, kp_, ql_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
+    convert_field(op_, wop_.data, wop_.norm, kp_, wl_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
+  }
+  B.norm2(ref(ql_), S_.qq, st_);
+  cg_alpha_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+  B.axpby(S_.alpha, ref(pl_), nullptr, ref(xl_), st_);                  // x += a p
+  B.axpby_norm(S_.nalpha, ref(ql_), nullptr, ref(sl_), S_.ss, st_);      // s -= a q
+  B.axpby_norm(S_.nalpha, ref(wl_), nullptr, ref(rl_), S_.rr_new, st_);  // r -= a w
+  cg_beta_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_, delta2_);
+  B.axpby(nullptr, ref(rl_), S_.beta, ref(pl_), st_);  // p = r + b p
+}
+
+void SlotEngine::bicg_iteration() {
+  Blas& B = s_.blas();
+  op_apply(ql_, pl_, 0, S_.active);  // v = Mhat p
+  B.cdot(ref(r0l_), ref(ql_), S_.tmp1, st_);
+  bicg_alpha_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+  B.axpby(S_.nalpha, ref(ql_), nullptr, ref(sl_), st_);  // s = r - alpha v (sl holds r)
+  op_apply(wl_, sl_, 0, S_.active);                       // t = Mhat s
+  B.cdot(ref(wl_), ref(sl_), S_.tmp1, st_);
+  B.norm2(ref(wl_), S_.qq, st_);
+  bicg_omega_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+  B.axpbypcz(S_.alpha, ref(pl_), S_.omega, ref(sl_), nullptr, ref(xl_), st_);  // x += alpha p + omega s
+  B.axpby_norm(S_.nomega, ref(wl_), nullptr, ref(sl_), S_.ss, st_);            // r = s - omega t
+  B.cdot(ref(r0l_), ref(sl_), S_.tmp2, st_);
+  bicg_beta_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_, delta2_);
+  B.axpbypcz(S_.one, ref(sl_), S_.nbo, ref(ql_), S_.beta, ref(pl_), st_);  // p = r + beta p - beta omega v
+}
+
+void SlotEngine::run_chunk(int k) {
+  QCU_CHECK_CUDA(cudaMemsetAsync(S_.status, 0, sizeof(int) * 4, st_));
+  if (q_.use_graph && k == chunk_) {
+    if (!graph_exec_) {
+      // kernel shapes are tuned in the first (eager) chunk; later chunks replay a graph
+      if (!warm_) {
+        for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
+        warm_ = true;
+        return;
       }
-    }
-    if (any_active) reliable_update(false);
-    // x_o = b_o + kappa D_oe x_e
-    s_.hop(xo_, xh_, bo_, 1, 0, q_.kappa, 1.0);
-    unpack_fermions(PREC_DOUBLE, s_.N, px, q_.src_mode, 0, xh_.data, nullptr, s_.geo, n_, st_);
-    unpack_fermions(PREC_DOUBLE, s_.N, px, q_.src_mode, 1, xo_.data, nullptr, s_.geo, n_, st_);
-    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-    res.iterations = iters;
-    res.true_residual.resize(n_);
-    res.converged = converged_;
-    for (int r = 0; r < n_; r++) res.true_residual[r] = std::sqrt(ss_true_host_[r] / bb_host_[r]);
-    res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    return res;
-  }
-
- private:
-  // out = Mhat in (dagger 0) or Mhat^dag in (dagger 1), fields in precision `prec`
-  void apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, int dagger, const int* mask) {
-    s_.hop(tmp, in, FieldView{}, 1, dagger, 1.0, 0.0, mask);
-    s_.hop(out, tmp, in, 0, dagger, -kappa2_, 1.0, mask);
-  }
-
-  // Krylov-precision q = Mhat p (and w = Mhat^dag q when want_w)
-  void op_apply(const FieldView& out_kp, const FieldView& in_kp, int dagger, const FieldView* chain_out = nullptr) {
-    if (op_ == kp_) {
-      apply_mhat(out_kp, in_kp, tmpop_, dagger, S_.active);
-    } else {
-      convert_field(kp_, in_kp.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_);
-      apply_mhat(qop_, pop_, tmpop_, dagger, S_.active);
-      convert_field(op_, qop_.data, qop_.norm, kp_, out_kp.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_);
-    }
-    (void)chain_out;
-  }
-
-  // CG step pieces: q = Mhat p, w = Mhat^dag q (reusing the operator-precision q)
-  void cg_apply() {
-    if (op_ == kp_) {
-      apply_mhat(ql_, pl_, tmpop_, 0, S_.active);
-      apply_mhat(wl_, ql_, tmpop_, 1, S_.active);
-    } else {
-      convert_field(kp_, pl_.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_);
-      apply_mhat(qop_, pop_, tmpop_, 0, S_.active);
-      apply_mhat(wop_, qop_, tmpop_, 1, S_.active);
-      convert_field(op_, qop_.data, qop_.norm, kp_, ql_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_);
-      convert_field(op_, wop_.data, wop_.norm, kp_, wl_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_);
-    }
-  }
-
-  void cg_iteration() {
-    Blas& B = s_.blas();
-    cg_apply();
-    B.norm2(ref(ql_, s_), S_.qq, st_);
-    cg_alpha_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
-    B.axpby(S_.alpha, ref(pl_, s_), nullptr, ref(xl_, s_), st_);               // x += a p
-    B.axpby_norm(S_.nalpha, ref(ql_, s_), nullptr, ref(sl_, s_), S_.ss, st_);  // s -= a q
-    B.axpby_norm(S_.nalpha, ref(wl_, s_), nullptr, ref(rl_, s_), S_.rr_new, st_);  // r -= a w
-    cg_beta_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_, delta2_);
-    B.axpby(nullptr, ref(rl_, s_), S_.beta, ref(pl_, s_), st_);  // p = r + b p
-  }
-
-  void bicg_iteration() {
-    Blas& B = s_.blas();
-    // v = Mhat p (into ql)
-    op_apply(ql_, pl_, 0);
-    B.cdot(ref(r0l_, s_), ref(ql_, s_), S_.tmp1, st_);
-    bicg_alpha_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
-    // s = r - alpha v   (in place on sl, which holds r)
-    B.axpby(S_.nalpha, ref(ql_, s_), nullptr, ref(sl_, s_), st_);
-    // t = Mhat s (into wl)
-    op_apply(wl_, sl_, 0);
-    B.cdot(ref(wl_, s_), ref(sl_, s_), S_.tmp1, st_);
-    B.norm2(ref(wl_, s_), S_.qq, st_);
-    bicg_omega_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
-    // x += alpha p + omega s
-    B.axpbypcz(S_.alpha, ref(pl_, s_), S_.omega, ref(sl_, s_), nullptr, ref(xl_, s_), st_);
-    // r = s - omega t  (sl becomes r)
-    B.axpby_norm(S_.nomega, ref(wl_, s_), nullptr, ref(sl_, s_), S_.ss, st_);
-    B.cdot(ref(r0l_, s_), ref(sl_, s_), S_.tmp2, st_);
-    bicg_beta_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_, delta2_);
-    // p = r + beta p - beta omega v
-    B.axpbypcz(ones_, ref(sl_, s_), S_.nbo, ref(ql_, s_), S_.beta, ref(pl_, s_), st_);
-  }
-
-  void run_chunk(int k) {
-    QCU_CHECK_CUDA(cudaMemsetAsync(S_.status, 0, sizeof(int) * 3, st_));
-    if (q_.use_graph && k == chunk_) {
-      if (!graph_exec_) {
-        // the kernel shapes must be tuned before capture; one eager chunk does it
-        if (!warm_) {
-          for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
-          warm_ = true;
-          return;
-        }
-        cudaGraph_t g;
-        QCU_CHECK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
-        try {
-          for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
-        } catch (...) {
-          cudaGraph_t dummy;
-          cudaStreamEndCapture(st_, &dummy);
-          if (dummy) cudaGraphDestroy(dummy);
-          throw;
-        }
-        QCU_CHECK_CUDA(cudaStreamEndCapture(st_, &g));
-        QCU_CHECK_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
-        QCU_CHECK_CUDA(cudaGraphDestroy(g));
+      cudaGraph_t g;
+      QCU_CHECK_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
+      } catch (...) {
+        cudaGraph_t dummy = nullptr;
+        cudaStreamEndCapture(st_, &dummy);
+        if (dummy) cudaGraphDestroy(dummy);
+        throw;
       }
-      QCU_CHECK_CUDA(cudaGraphLaunch(graph_exec_, st_));
+      QCU_CHECK_CUDA(cudaStreamEndCapture(st_, &g));
+      QCU_CHECK_CUDA(cudaGraphInstantiate(&graph_exec_, g, 0));
+      QCU_CHECK_CUDA(cudaGraphDestroy(g));
+    }
+    QCU_CHECK_CUDA(cudaGraphLaunch(graph_exec_, st_));
+  } else {
+    for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
+  }
+}
+
+// (Re)start the slots in `slots`: fold x_lo into x, recompute the true
+// residual s = bhat - Mhat x in FP64, decide convergence, and restart the
+// Krylov recurrence of the slots that go on.  `fresh` slots start from x = 0
+// with p = r.
+void SlotEngine::restart(const std::vector<int>& slots, bool fresh) {
+  if (slots.empty()) return;
+  Blas& B = s_.blas();
+  upload_sel(slots);
+  if (!fresh) B.axpby(S_.cm, ref(xl_), nullptr, ref(xh_), st_);  // x += x_lo
+  B.axpby(S_.zero, ref(xl_), S_.ck, ref(xl_), st_);              // x_lo = 0
+  if (fresh) {
+    B.axpby(S_.zero, ref(xh_), S_.ck, ref(xh_), st_);  // x = 0
+    B.axpby(S_.zero, ref(pl_), S_.ck, ref(pl_), st_);  // p = 0
+  }
+  // s = bhat - Mhat x  (only the selected slots are computed)
+  apply_mhat(th_, xh_, tmp64_, 0, S_.sel);
+  B.axpby(S_.cm, ref(bh_), S_.ck, ref(sh_), st_);
+  B.axpby_norm(S_.cn, ref(th_), nullptr, ref(sh_), S_.ss_true, st_);
+  std::vector<double> ss(n_);
+  QCU_CHECK_CUDA(cudaMemcpyAsync(ss.data(), S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
+  std::vector<int> act(n_);
+  QCU_CHECK_CUDA(cudaMemcpyAsync(act.data(), S_.active, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+  std::vector<int> go_on;
+  for (int r : slots) {
+    SlotState& h = host_[r];
+    h.true_res2 = ss[r];
+    h.updates += fresh ? 0 : 1;
+    if (verbose_)
+      fprintf(stderr, "qcu solver: slot %d %s after %d iterations, true |s|/|b| %.3e\n", r,
+              fresh ? "admitted" : "reliable update", h.iterations, std::sqrt(ss[r] / h.bb));
+    if (ss[r] <= h.stop2) {
+      h.phase = SlotState::DONE;
+      h.converged = 1;
+      act[r] = 0;
+    } else if (h.iterations >= q_.max_iter || !std::isfinite(ss[r])) {
+      h.phase = SlotState::DONE;
+      h.converged = 0;
+      act[r] = 0;
     } else {
-      for (int i = 0; i < k; i++) q_.solver == 0 ? cg_iteration() : bicg_iteration();
+      h.phase = SlotState::ACTIVE;
+      act[r] = 1;
+      go_on.push_back(r);
     }
   }
-
-  // x += x_lo; s = bhat - Mhat x in FP64; reset the Krylov residuals.
-  // Returns whether any RHS is still unconverged.
-  bool reliable_update(bool first) {
-    Blas& B = s_.blas();
-    if (!first) {
-      B.add_to(ref(xl_, s_), ref(xh_, s_), st_);
-      B.zero(ref(xl_, s_), st_);
-    }
-    // s = bhat - Mhat x
-    apply_mhat(th_, xh_, tmp64_, 0, nullptr);
-    B.copy(ref(bh_, s_), ref(sh_, s_), st_);
-    B.axpby_norm(mones_, ref(th_, s_), nullptr, ref(sh_, s_), S_.ss_true, st_);
-    ss_true_host_.resize(n_);
-    QCU_CHECK_CUDA(cudaMemcpyAsync(ss_true_host_.data(), S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.active, act.data(), sizeof(int) * n_, cudaMemcpyHostToDevice, st_));
+  if (go_on.empty()) {
     QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-    std::vector<int> act(n_);
-    bool any = false;
-    for (int r = 0; r < n_; r++) {
-      converged_[r] = ss_true_host_[r] <= stop2_host_[r] ? 1 : 0;
-      act[r] = converged_[r] ? 0 : 1;
-      any |= act[r] != 0;
-    }
-    if (verbose_) {
-      fprintf(stderr, "qcu solver: reliable update %d, true |s|/|b| per RHS:", updates_);
-      for (int r = 0; r < n_; r++) fprintf(stderr, " %.3e", std::sqrt(ss_true_host_[r] / bb_host_[r]));
-      fprintf(stderr, "\n");
-    }
-    updates_++;
-    QCU_CHECK_CUDA(cudaMemcpyAsync(S_.active, act.data(), sizeof(int) * n_, cudaMemcpyHostToDevice, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(S_.maxss, S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(S_.ss, S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToDevice, st_));
-    // Krylov residuals in the low precision
-    B.copy(ref(sh_, s_), ref(sl_, s_), st_);
-    if (q_.solver == 0) {
-      op_apply(rl_, sl_, 1);  // r = Mhat^dag s
-      B.norm2(ref(rl_, s_), S_.rr, st_);
-      if (!first) {
-        B.cdot(ref(rl_, s_), ref(pl_, s_), S_.tmp1, st_);
-        cg_restore_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
-        B.axpby(S_.tmp2, ref(rl_, s_), nullptr, ref(pl_, s_), st_);  // p += c r
-      }
-    }
-    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-    return any;
+    return;
   }
-
-  Session& s_;
-  int n_;
-  SolveRequest q_;
-  int kp_, op_;
-  double kappa2_, delta2_;
-  cudaStream_t st_;
-  FieldView be_, bo_, bh_, xh_, xo_, sh_, th_, tmp64_;
-  FieldView xl_, sl_, rl_, pl_, ql_, wl_, r0l_;
-  FieldView pop_, qop_, wop_, tmpop_;
-  Scalars S_;
-  double2 *ones_, *mones_, *kap_;
-  std::vector<double> stop2_host_, bb_host_, ss_true_host_;
-  std::vector<int> converged_;
-  cudaGraphExec_t graph_exec_ = nullptr;
-  bool warm_ = false;
-  bool verbose_ = getenv("QCU_SOLVER_VERBOSE") != nullptr;
-  int updates_ = 0;
-  int chunk_ = getenv("QCU_SOLVER_CHUNK") ? std::max(1, atoi(getenv("QCU_SOLVER_CHUNK"))) : kChunk;
-
-  // per-chunk scalars of RHS 0 (QCU_SOLVER_VERBOSE)
-  void trace(int iters, const int* status) {
-    double v[5];
-    double2 c[2];
-    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[0], S_.rr, sizeof(double), cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[1], S_.qq, sizeof(double), cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(&v[2], S_.ss, sizeof(double), cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(&c[0], S_.alpha, sizeof(double2), cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaMemcpyAsync(&c[1], S_.beta, sizeof(double2), cudaMemcpyDeviceToHost, st_));
-    QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
-    fprintf(stderr, "qcu solver: iter %d active %d update %d | rhs0 rr %.3e qq %.3e ss/bb %.3e alpha %.3e beta %.3e\n",
-            iters, status[0], status[1], v[0], v[1], v[2] / bb_host_[0], c[0].x, c[1].x);
+  upload_sel(go_on);
+  B.axpby(S_.cm, ref(sh_), S_.ck, ref(sl_), st_);  // s_lo = s
+  if (q_.solver == 0) {
+    op_apply(rl_, sl_, 1, S_.sel);  // r = Mhat^dag s
+    B.norm2(ref(rl_), S_.rr_new, st_);
+    B.cdot(ref(rl_), ref(pl_), S_.tmp1, st_);
+    restart_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
+    B.axpby(S_.tmp2, ref(rl_), nullptr, ref(pl_), st_);  // p += c r
+  } else {
+    B.axpby(S_.cm, ref(sl_), S_.ck, ref(r0l_), st_);  // shadow residual r0 = r
+    B.axpby(S_.cm, ref(sl_), S_.ck, ref(pl_), st_);   // p = r
+    B.cdot(ref(r0l_), ref(sl_), S_.tmp1, st_);
+    bicg_restart_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
   }
-};
+  QCU_CHECK_CUDA(cudaGetLastError());
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+}
 
-}  // namespace
+void SlotEngine::admit(const std::vector<int>& slots, void* const* b, const double* kappa, const double* tol,
+                       int src_mode) {
+  if (slots.empty()) return;
+  Blas& B = s_.blas();
+  PtrArray pb{};
+  for (size_t i = 0; i < slots.size(); i++) {
+    const int r = slots[i];
+    QCU_REQUIRE(r >= 0 && r < n_ && host_[r].phase == SlotState::FREE, QCU_ERR_INVALID_ARGUMENT,
+                "admit: slot is not free");
+    QCU_REQUIRE(tol[i] > 0 && kappa[i] > 0, QCU_ERR_INVALID_ARGUMENT, "kappa and tol must be positive");
+    pb.p[r] = b[i];
+    SlotState& h = host_[r];
+    h = SlotState{};
+    h.kappa = kappa[i];
+    h.tol = tol[i];
+    h.phase = SlotState::ACTIVE;
+  }
+  upload_kappa();
+  pack_fermions(PREC_DOUBLE, s_.N, pb, src_mode, 0, be_.data, nullptr, s_.geo, n_, st_);
+  pack_fermions(PREC_DOUBLE, s_.N, pb, src_mode, 1, bo_.data, nullptr, s_.geo, n_, st_);
+  // |b|^2 over both parities; the slot stops when |s|^2 <= tol^2 |b|^2
+  B.norm2(ref(be_), S_.bb, st_);
+  B.norm2(ref(bo_), S_.bo2, st_);
+  std::vector<double> bb(n_), bo2(n_), stop2(n_);
+  QCU_CHECK_CUDA(cudaMemcpyAsync(bb.data(), S_.bb, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(bo2.data(), S_.bo2, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(stop2.data(), S_.stop2, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+  for (int r : slots) {
+    SlotState& h = host_[r];
+    h.bb = bb[r] + bo2[r];
+    if (!(h.bb > 0)) h.bb = 1.0;  // a zero source: x = 0 is exact
+    h.stop2 = h.tol * h.tol * h.bb;
+    stop2[r] = h.stop2;
+  }
+  QCU_CHECK_CUDA(cudaMemcpyAsync(S_.stop2, stop2.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, st_));
+  // bhat = b_e + kappa_r D_eo b_o for the new slots
+  upload_sel(slots);
+  s_.hop(bh_, bo_, be_, 0, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  restart(slots, true);
+}
+
+std::vector<int> SlotEngine::step() {
+  std::vector<int> finished;
+  for (int r = 0; r < n_; r++)
+    if (host_[r].phase == SlotState::DONE && !host_[r].reported) {
+      host_[r].reported = true;
+      finished.push_back(r);
+    }
+  if (active_slots() == 0) return finished;
+  const int k = chunk_;
+  run_chunk(k);
+  std::vector<int> act(n_), upd(n_);
+  QCU_CHECK_CUDA(cudaMemcpyAsync(act.data(), S_.active, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaMemcpyAsync(upd.data(), S_.upd, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+  std::vector<int> sel;
+  for (int r = 0; r < n_; r++) {
+    if (host_[r].phase != SlotState::ACTIVE) continue;
+    host_[r].iterations += k;
+    if (upd[r] || !act[r] || host_[r].iterations >= q_.max_iter) sel.push_back(r);
+  }
+  restart(sel, false);
+  for (int r : sel)
+    if (host_[r].phase == SlotState::DONE && !host_[r].reported) {
+      host_[r].reported = true;
+      finished.push_back(r);
+    }
+  return finished;
+}
+
+void SlotEngine::retire(const std::vector<int>& slots, void* const* x, int src_mode) {
+  if (slots.empty()) return;
+  PtrArray px{};
+  for (size_t i = 0; i < slots.size(); i++) {
+    const int r = slots[i];
+    QCU_REQUIRE(r >= 0 && r < n_ && host_[r].phase == SlotState::DONE, QCU_ERR_INVALID_ARGUMENT,
+                "retire: slot has not finished");
+    px.p[r] = x[i];
+  }
+  upload_sel(slots);
+  // x_o = b_o + kappa_r D_oe x_e
+  s_.hop(xo_, xh_, bo_, 1, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  unpack_fermions(PREC_DOUBLE, s_.N, px, src_mode, 0, xh_.data, nullptr, s_.geo, n_, st_);
+  unpack_fermions(PREC_DOUBLE, s_.N, px, src_mode, 1, xo_.data, nullptr, s_.geo, n_, st_);
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+  for (int r : slots) host_[r].phase = SlotState::FREE;
+}
 
 SolveResult solve(Session& s, void* const* x, void* const* b, int nrhs, const SolveRequest& req) {
   QCU_REQUIRE(nrhs >= 1 && nrhs <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
-  QCU_REQUIRE(req.solver == 0 || req.solver == 1, QCU_ERR_INVALID_ARGUMENT, "unknown solver");
-  QCU_REQUIRE(prec_valid(req.inner_prec), QCU_ERR_INVALID_ARGUMENT, "bad inner precision");
   QCU_REQUIRE(req.tol > 0 && req.max_iter > 0, QCU_ERR_INVALID_ARGUMENT, "tol and max_iter must be positive");
   QCU_REQUIRE(req.src_mode == SRC_EO_FULL || req.src_mode == SRC_LEX, QCU_ERR_INVALID_ARGUMENT,
               "solver fields must be full eo or lexicographic");
-  Solver sv(s, nrhs, req);
-  return sv.run(x, b);
+  auto t0 = std::chrono::steady_clock::now();
+  SlotEngine eng(s, nrhs, req, "sv");
+  std::vector<int> slots(nrhs);
+  std::vector<double> kap(nrhs, req.kappa), tol(nrhs, req.tol);
+  for (int r = 0; r < nrhs; r++) slots[r] = r;
+  eng.admit(slots, b, kap.data(), tol.data(), req.src_mode);
+  int chunks = 0;
+  while (eng.active_slots() > 0) {
+    eng.step();
+    chunks++;
+  }
+  eng.retire(slots, x, req.src_mode);
+  SolveResult res;
+  res.true_residual.resize(nrhs);
+  res.converged.resize(nrhs);
+  for (int r = 0; r < nrhs; r++) {
+    const SlotState& h = eng.slot(r);
+    res.true_residual[r] = std::sqrt(h.true_res2 / h.bb);
+    res.converged[r] = h.converged;
+    res.iterations = std::max(res.iterations, h.iterations);
+    res.reliable_updates = std::max(res.reliable_updates, h.updates);
+  }
+  res.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  (void)chunks;
+  return res;
 }
 
 }  // namespace qcu

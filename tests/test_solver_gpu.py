@@ -84,6 +84,25 @@ def test_masks_uneven_rhs(cuda, qcu_lib):
     assert rel(x[2], 1e6 * x[3]) < 1e-8
 
 
+@pytest.mark.parametrize("inner", [1, 0])
+def test_slot_independence(cuda, qcu_lib, inner):
+    """A slot's iterates do not depend on what the other slots hold: RHS 0 of
+    [bX, bY, bY'] and of [bX, bZ, bZ'] are solved bit-identically, although
+    the other slots take different iteration counts and reliable-update
+    times (which restart those slots in the middle of RHS 0's solve)."""
+    torch, Q = cuda, qcu_lib
+    L, n, kappa, tol = (4, 4, 4, 8), 3, 0.12, 1e-10
+    setup(torch, Q, L, n, 235)
+    b = S.random_fermions(L, n, 5, seed=236, parities=2)
+    b[2] *= 1e-4
+    b[4, :, :4] = 0.0  # a source with a different spectrum
+    x1, p1 = solve(torch, Q, b[[0, 1, 2]], kappa=kappa, tol=tol, inner_precision=inner)
+    x2, p2 = solve(torch, Q, b[[0, 3, 4]], kappa=kappa, tol=tol, inner_precision=inner)
+    assert p1.converged[0] == 1 and p2.converged[0] == 1
+    assert np.array_equal(x1[0], x2[0])
+    assert p1.true_residual[0] == p2.true_residual[0]
+
+
 def test_graph_and_eager_agree(cuda, qcu_lib):
     torch, Q = cuda, qcu_lib
     L, n, kappa = (4, 4, 4, 4), 3, 0.12
