@@ -18,7 +18,12 @@ Reported (one JSON line on rank 0):
   roofline   algorithmic bytes per launch / mean launch time vs measured HBM
   cpu_baseline  the FP64 OpenMP oracle dslash on this host's cores
   sweep      site*RHS/s and roofline fraction per precision x nrhs
+  fma_peaks  measured FP64 / FP32 FMA peaks (the FP64 dslash is FP64-pipe-bound)
   solve      eo-CG to FP64 true residual 1e-10: mixed precision vs plain FP64
+  serve      Poisson request stream over 4 resident gauges: p50/p99, solves/s
+             vs serial plain-FP64 solves
+  colors     16^3x32 SU(N), N = 4, 6, 8, nrhs 16-64 (FP32 / BF16), and a
+             masked BiCGStab per N
 
 --impl reference times the reference's CPU path for this operator on the
 host cores.  The reference has no CPU implementation (its only code path is
@@ -170,6 +175,12 @@ def dist_setup():
     return 1, 0, 0, None
 
 
+def job_throughput(units_per_rank: float, world: int, ms_max: float) -> float:
+    """Whole-job units per second: every rank processes units_per_rank in
+    its step; the step time is the maximum over ranks."""
+    return units_per_rank * world / (ms_max * 1e-3)
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -279,7 +290,7 @@ def run_gpu(args):
     ms_local = e0.elapsed_time(e1) / args.steps
     ms = max_over_ranks(dist, ms_local)
     units = vh * nrhs
-    value = units * world / (ms * 1e-3)
+    value = job_throughput(units, world, ms)
     peak, peak_kind = measured_peaks()
     bpu = bytes_per_site_rhs(prec, n, nrhs)
     achieved = bpu * units / (ms_local * 1e-3) / 1e9
@@ -327,7 +338,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         ems = max_over_ranks(dist, f0.elapsed_time(f1) / e2e_steps)
         bytes_io = nrhs * vh * 4 * n * 16
-        e2e = {"value": units * world / (ems * 1e-3), "unit": "site*RHS/s", "h2d_bytes_per_step": bytes_io,
+        e2e = {"value": job_throughput(units, world, ems), "unit": "site*RHS/s", "h2d_bytes_per_step": bytes_io,
                "d2h_bytes_per_step": bytes_io, "ms_per_step": round(ems, 3), "steps": e2e_steps,
                "path": "pinned host -> pushBackFermions x12 -> startDslash -> pinned host (FP64 caller layout)"}
         Q.set_stream(None)
@@ -338,7 +349,12 @@ def run_gpu(args):
 
     # ---- sweep of precisions x nrhs ------------------------------------
     sweep = []
+    fma = None
     if not args.skip_sweep and rank == 0:
+        # FMA pipe peaks: FP64 bounds the FP64 dslash (1320 flop vs 480 B per site*RHS at nrhs 12)
+        fma = {"fp64_tflops": round(Q.measure_fma_rate(Q.QCU_DOUBLE_PRECISION), 2),
+               "fp32_tflops": round(Q.measure_fma_rate(Q.QCU_SINGLE_PRECISION), 2),
+               "how": "8 independent FMA chains per thread, 8 blocks of 256 per SM, CUDA events"}
         for p, sname in ((2, "fp64"), (1, "fp32"), (0, "fp16"), (4, "bf16")):
             for nr in (1, 4, 12, 24):
                 if p == 2 and nr == 24:
@@ -349,6 +365,8 @@ def run_gpu(args):
                               "site_rhs_per_s": round(u / (ms_s * 1e-3)),
                               "gbs": round(ach, 1), "hbm_frac": round(ach / peak, 4),
                               "gflops": round(FLOPS_PER_SITE_RHS(n) * u / (ms_s * 1e-3) / 1e9, 1)})
+                if p == 2:
+                    sweep[-1]["fp64_pipe_frac"] = round(sweep[-1]["gflops"] / (1e3 * fma["fp64_tflops"]), 4)
         torch.cuda.empty_cache()
 
     # ---- CPU baseline (oracle, FP64, host cores) -----------------------
@@ -366,6 +384,11 @@ def run_gpu(args):
     if rank == 0 and not args.skip_serve:
         serve = serve_bench(torch, Q)
 
+    # ---- SU(N), N = 4..8, large nrhs ----------------------------------------
+    colors = None
+    if rank == 0 and not args.skip_colors:
+        colors = colors_bench(torch, Q, peak, fma)
+
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -377,7 +400,7 @@ def run_gpu(args):
                        "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
             "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
-            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "solve": solve, "serve": serve,
+            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve, "colors": colors,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -440,6 +463,60 @@ def solve_bench(torch, Q):
         out["speedup_fp32_inner_vs_fp64"] = round(out["fp64_plain"]["seconds"] / out["fp32_inner"]["seconds"], 2)
         out["speedup_fp16_inner_vs_fp64"] = round(out["fp64_plain"]["seconds"] / out["fp16_inner"]["seconds"], 2)
     return out
+
+
+def colors_bench(torch, Q, peak, fma):
+    """16^3x32, SU(N) N = 4, 6, 8, nrhs 16 / 32 / 64, FP32 and BF16 storage
+    (FP32 arithmetic): dslash throughput against the HBM roofline and the FP32
+    FMA peak (at N = 8 the CUDA-core kernel is compute-bound), and one
+    BiCGStab solve per N with per-RHS masks (one source 1e-4 times smaller,
+    one zero) to 1e-8."""
+    from mrhs_qcu_gb300 import synthetic as S
+    L = (16, 16, 16, 32)
+    vh = S.half_volume(L)
+    rows, solves = [], []
+    for n in (4, 6, 8):
+        g_dev, psi = make_inputs(torch, L, n, 64, seed_g=300 + n, seed_p=301)
+        for p, pname in ((1, "fp32"), (4, "bf16")):
+            for nr in (16, 32, 64):
+                ms_s, u = time_resident(torch, Q, L, n, nr, p, 10, 3, g_dev, psi)
+                rate = u / (ms_s * 1e-3)
+                gbs = bytes_per_site_rhs(p, n, nr) * rate / 1e9
+                tf = FLOPS_PER_SITE_RHS(n) * rate / 1e12
+                rows.append({"N": n, "precision": pname, "nrhs": nr, "ms": round(ms_s, 4),
+                             "site_rhs_per_s": round(rate), "gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+                             "tflops": round(tf, 2),
+                             "fp32_fma_frac": round(tf / fma["fp32_tflops"], 4) if fma else None})
+        # BiCGStab with masks: 16 RHS, FP32 inner
+        nr = 16
+        b = torch.complex(torch.randn((nr, 2, vh, 4, n), device="cuda", dtype=torch.float64,
+                                      generator=torch.Generator(device="cuda").manual_seed(302)),
+                          torch.randn((nr, 2, vh, 4, n), device="cuda", dtype=torch.float64,
+                                      generator=torch.Generator(device="cuda").manual_seed(303)))
+        b[1] *= 1e-4
+        b[2] = 0
+        x = torch.zeros_like(b)
+        Q.initGridSize(L, n)
+        Q.set_antiperiodic_t(True)
+        Q.loadQcuGauge(g_dev.data_ptr())
+        prm = Q.solver_params(kappa=0.11, tol=1e-8, inner_precision=Q.QCU_SINGLE_PRECISION,
+                              solver=Q.QCU_SOLVER_BICGSTAB, max_iter=5000)
+        for phase in ("cold", "warm"):
+            x.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Q.invert([x[r].data_ptr() for r in range(nr)], [b[r].data_ptr() for r in range(nr)], prm,
+                     raise_on_error=False)
+            torch.cuda.synchronize()
+            sec = time.perf_counter() - t0
+        solves.append({"N": n, "nrhs": nr, "seconds": round(sec, 4), "iterations": prm.iterations,
+                       "max_true_residual": max(prm.true_residual[r] for r in range(nr)),
+                       "all_converged": all(prm.converged[r] for r in range(nr))})
+        del g_dev, psi, b, x
+        torch.cuda.empty_cache()
+    return {"workload": "16^3x32 SU(N) dslash (CUDA cores, FP32 arithmetic); BiCGStab kappa 0.11, FP32 inner, "
+                        "16 RHS (one 1e-4 smaller, one zero) to 1e-8",
+            "dslash": rows, "bicgstab": solves}
 
 
 def serve_bench(torch, Q, n_requests=48, rate=60.0, serial_budget_s=8.0):
@@ -566,6 +643,7 @@ def main():
     ap.add_argument("--skip-sweep", action="store_true")
     ap.add_argument("--skip-solve", action="store_true")
     ap.add_argument("--skip-serve", action="store_true")
+    ap.add_argument("--skip-colors", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -576,7 +654,8 @@ def main():
                     help="headline kernel only (no e2e, sweep, CPU or solve legs), for ncu captures")
     args = ap.parse_args()
     if args.profile:
-        args.skip_sweep = args.skip_solve = args.skip_serve = args.skip_cpu = args.skip_e2e = True
+        args.skip_sweep = args.skip_solve = args.skip_serve = args.skip_colors = args.skip_cpu = True
+        args.skip_e2e = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

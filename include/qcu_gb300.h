@@ -123,15 +123,22 @@ int qcuNorm2MRHS(double *out, const void *field, int precision, int nrhs);
 int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_elements, int nrhs, void *stream);
 
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
- * Returns the chosen RHS-per-thread, block size and register-cap variant
- * (minimum resident 256-thread blocks per SM) and whether the packed FP32x2
- * arithmetic variant was chosen. */
-int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *min_blocks, int *packed);
+ * Returns the chosen RHS-per-thread, block size, register-cap variant
+ * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
+ * 6 = 104) and whether the packed FP32x2 arithmetic variant was chosen. */
+int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed);
 
-/* The compiled dslash kernel shapes for (precision, nColors): *count triples
- * (RHS per thread, min_blocks, packed) are available; the first max_shapes
- * are written to shapes[3 * i .. 3 * i + 2].  Any of them can be pinned with
- * QCU_DSLASH_CONFIG="R,block,min_blocks,packed". */
+/* No counterpart in the reference.  FMA throughput of the current GPU in
+ * TFLOP/s (2 flop per FMA), precision QCU_DOUBLE_PRECISION or
+ * QCU_SINGLE_PRECISION: the peak that bounds compute-bound kernels such as
+ * the FP64 dslash.  Synchronous; takes a few milliseconds. */
+int qcuMeasureFmaRate(int precision, double *tflops);
+
+/* The compiled dslash kernel shapes for (precision, nColors): *count
+ * quadruples (RHS per thread, register-cap variant, packed, stages) are
+ * available; the first max_shapes are written to shapes[4 * i .. 4 * i + 3].
+ * stages > 0 is the TMA-staged kernel with that many ring buffers.  Any shape
+ * can be pinned with QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages". */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 
 typedef struct QcuSolverParam_s {

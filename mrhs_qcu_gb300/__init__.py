@@ -73,7 +73,7 @@ ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge"
 EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
-               "qcuTuneDslash", "qcuDslashKernels", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
+               "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
                "qcuNorm2MRHSNoAlloc",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
@@ -133,6 +133,7 @@ def lib() -> ctypes.CDLL:
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
         "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
+        "qcuMeasureFmaRate": ([I, ctypes.POINTER(ctypes.c_double)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
         "qcuNorm2MRHS": ([P, P, I, I], I),
@@ -309,11 +310,19 @@ def tune_dslash(nrhs: int, precision: int):
 
 
 def dslash_kernels(precision: int, n_colors: int = 3):
-    """Compiled dslash kernel shapes [(R, min_blocks, packed), ...]."""
-    arr = (ctypes.c_int * (3 * 64))()
+    """Compiled dslash kernel shapes [(R, reg_cap, packed, stages), ...];
+    stages > 0 is the TMA-staged kernel."""
+    arr = (ctypes.c_int * (4 * 64))()
     cnt = ctypes.c_int()
     _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
-    return [tuple(arr[3 * i:3 * i + 3]) for i in range(min(cnt.value, 64))]
+    return [tuple(arr[4 * i:4 * i + 4]) for i in range(min(cnt.value, 64))]
+
+
+def measure_fma_rate(precision: int) -> float:
+    """FMA throughput of the current GPU in TFLOP/s (FP64 or FP32)."""
+    v = ctypes.c_double()
+    _raise_if(lib().qcuMeasureFmaRate(int(precision), ctypes.byref(v)))
+    return v.value
 
 
 def solver_params(**kw) -> QcuSolverParam:

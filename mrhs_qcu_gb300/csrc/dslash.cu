@@ -3,6 +3,7 @@
 #include <mutex>
 
 #include "dslash.h"
+#include "dslash_tma.h"
 
 namespace qcu {
 namespace {
@@ -42,7 +43,37 @@ int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max) {
   return n;
 }
 
-void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st) {
+bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg) {
+  if (cfg.tma <= 0 || A.nrhs % cfg.R || !find_tma(prec, N, cfg.R, cfg.tma) || !tma_pointers_ok(A)) return false;
+  TmaDslashArgs T;
+  int threads = 0;
+  size_t smem = 0;
+  return tma_plan(prec, N, A.geo, A.nrhs, cfg.R, cfg.tma, cfg.rcta, &T, &threads, &smem);
+}
+
+void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
+  DslashConfig cfg = cfg_in;
+  if (cfg.tma > 0) {
+    if (tma_runs(A, prec, N, cfg)) {
+      QCU_REQUIRE((int64_t)A.geo.vh * A.nrhs * prec_complex_bytes(prec) < (1ll << 32), QCU_ERR_INVALID_ARGUMENT,
+                  "field component stride must stay below 4 GB");
+      DslashArgs B = A;
+      B.af = (float)A.a;
+      B.bf = (float)A.b;
+      find_tma(prec, N, cfg.R, cfg.tma)(B, cfg.rcta, st);
+      QCU_CHECK_CUDA(cudaGetLastError());
+      return;
+    }
+    // arguments the staged kernel cannot take (e.g. a misaligned caller buffer): register kernel
+    cfg = DslashConfig{};
+    int opts[8];
+    const int n = dslash_r_options(prec, N, opts, 8);
+    for (int i = 0; i < n; i++)
+      if (A.nrhs % opts[i] == 0 && opts[i] <= 2) {
+        cfg.R = opts[i];
+        break;
+      }
+  }
   DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk);
   QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
               std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +

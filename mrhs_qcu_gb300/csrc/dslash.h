@@ -13,7 +13,7 @@ namespace qcu {
 using DslashLauncher = void (*)(const DslashArgs&, int block, cudaStream_t);
 
 // registry filled by the instantiation units (dslash_inst_*.cu); minb is the
-// register-cap variant (minimum resident 256-thread blocks per SM)
+// register-cap variant of the kernel (RegCap in dslash_kernel.cuh)
 // pk selects the packed FP32x2 arithmetic variant
 DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0);
 void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn);
@@ -28,7 +28,12 @@ struct DslashConfig {
   int block = 128;  // <= 256 (launch bounds)
   int minb = 1;
   int pk = 0;
+  int tma = 0;   // > 0: the TMA-staged kernel (dslash_tma.cuh) with this many ring stages
+  int rcta = 0;  // its RHS per tile (0: the largest that fits)
 };
+
+// whether the staged kernel of cfg can run these arguments
+bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg);
 
 // launch with an explicit configuration (throws if not compiled)
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st);

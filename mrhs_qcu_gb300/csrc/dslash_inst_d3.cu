@@ -10,6 +10,7 @@ struct Register_d3 {
     register_dslash(PREC_DOUBLE, 3, 2, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 2, 1, false>);
     register_dslash(PREC_DOUBLE, 3, 3, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 3, 1, false>);
     register_dslash(PREC_DOUBLE, 3, 4, 1, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 4, 1, false>);
+    register_dslash(PREC_DOUBLE, 3, 1, 4, 0, &launch_wilson_mrhs<PREC_DOUBLE, 3, 1, 4, false>);
   }
 } register_d3;
 }  // namespace

@@ -90,6 +90,25 @@ struct Vec {
       for (int i = 0; i < nv; i++) d[i] = __ldg(q + i);
     }
   }
+  // the same from shared memory (plain loads)
+  __device__ __forceinline__ static void load_shared(const E* p, E (&v)[R]) {
+    if constexpr (vbytes == 16) {
+      const uint4* q = reinterpret_cast<const uint4*>(p);
+      uint4* d = reinterpret_cast<uint4*>(v);
+#pragma unroll
+      for (int i = 0; i < nv; i++) d[i] = q[i];
+    } else if constexpr (vbytes == 8) {
+      const uint2* q = reinterpret_cast<const uint2*>(p);
+      uint2* d = reinterpret_cast<uint2*>(v);
+#pragma unroll
+      for (int i = 0; i < nv; i++) d[i] = q[i];
+    } else {
+      const unsigned* q = reinterpret_cast<const unsigned*>(p);
+      unsigned* d = reinterpret_cast<unsigned*>(v);
+#pragma unroll
+      for (int i = 0; i < nv; i++) d[i] = q[i];
+    }
+  }
   __device__ __forceinline__ static void store(E* p, const E (&v)[R]) {
     if constexpr (vbytes == 16) {
       uint4* q = reinterpret_cast<uint4*>(p);
@@ -438,85 +457,19 @@ __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK
 
 }  // namespace detail
 
-// MINB: minimum resident blocks of 256 threads per SM requested from the
-// compiler, i.e. a register cap of 65536 / (256 * MINB) per thread (1: 255).
-// PK: FP32 arithmetic on the packed FP32x2 pipe (FP32 / 16-bit storage only).
-template <int P, int N, int R, int MINB, bool PK>
-__global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs A) {
+namespace detail {
+
+// Epilogue of both hop kernels: out = a_r * acc + b * x for one site and R
+// RHS (a_r per RHS when a_rhs_f / a_rhs_d is given), written in the storage
+// precision; 16-bit storage also writes the per-(site, RHS) scale.
+template <int P, int N, int R>
+__device__ __forceinline__ void store_out(C2<typename Store<P>::real> (&acc)[4][N][R], const DslashArgs& A,
+                                          uint32_t site, uint32_t rhs0) {
   using S = Store<P>;
   using T = typename S::real;
   using E = typename S::elem;
-  using namespace detail;
-  static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
-
-  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t site, grp;
-  A.div_groups.divmod(gid, site, grp);
-  if (site >= (uint32_t)A.geo.vh) return;
-  const uint32_t rhs0 = grp * R;
-  if (A.mask) {
-    bool any = false;
-#pragma unroll
-    for (int r = 0; r < R; r++) any |= A.mask[rhs0 + r] != 0;
-    if (!any) return;
-  }
-
-  uint32_t rest, xh, y, z, t;
-  A.geo.div_hx.divmod(site, rest, xh);
-  uint32_t rest2;
-  A.geo.div_y.divmod(rest, rest2, y);
-  A.geo.div_z.divmod(rest2, t, z);
-  const uint32_t hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
-  const uint32_t p = A.parity;
-  const uint32_t eo = (y + z + t) & 1u;
-  const T f = A.dagger ? (T)-1 : (T)1;
   const uint32_t vh = A.geo.vh;
   const uint32_t nrhs = A.nrhs;
-  const E* __restrict__ in = static_cast<const E*>(A.in);
-  const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
-  constexpr uint32_t NN = N * N;
-
-  HopAcc<T, N, R, PK> hacc;
-  hacc.zero();
-
-  // link offsets: forward links at (mu, p, site), backward at (mu, 1-p, nb)
-  const uint32_t lf = p * NN * vh + site;
-  const uint32_t lb = (1u - p) * NN * vh;
-  const uint32_t dmu = 2 * NN * vh;  // one direction's links
-  {  // X
-    const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
-    const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-    hop_any<P, N, R, PK, 0, true>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 0, false>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
-  }
-  {  // Y
-    const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
-    const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
-    hop_any<P, N, R, PK, 1, true>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 1, false>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
-  }
-  {  // Z
-    const uint32_t pl = A.geo.plane;
-    const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
-    const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
-    hop_any<P, N, R, PK, 2, true>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 2, false>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
-  }
-  {  // T, with the optional antiperiodic sign
-    const uint32_t cb = A.geo.cube;
-    const bool top = t == Lt - 1, bot = t == 0;
-    const uint32_t nf = top ? site - (Lt - 1) * cb : site + cb;
-    const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
-    const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
-    const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
-    hop_any<P, N, R, PK, 3, true>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
-    hop_any<P, N, R, PK, 3, false>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
-  }
-
-  C2<T> acc[4][N][R];
-  hacc.to_rows(acc);
-
-  // epilogue: out = a_r * acc + b * x, a_r per RHS when a_rhs is given
   T ca[R], cbx;
   if constexpr (sizeof(T) == 4) {
     cbx = A.bf;
@@ -603,6 +556,97 @@ __global__ void __launch_bounds__(256, MINB) wilson_mrhs_kernel(const DslashArgs
         Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v);
       }
   }
+}
+
+}  // namespace detail
+
+// MINB: register-cap variant of the kernel (registers per thread, and with
+// them the resident warps per SM, against spills):
+//   1: no cap (255), 2: 128, 3: 85, 4: 112, 5: 96, 6: 104.
+// 2 and 3 are the caps of 2 and 3 resident 256-thread blocks per SM.
+template <int MINB>
+struct RegCap {
+  static constexpr int regs =
+      MINB == 2 ? 128 : MINB == 3 ? 85 : MINB == 4 ? 112 : MINB == 5 ? 96 : MINB == 6 ? 104 : 255;
+};
+
+// PK: FP32 arithmetic on the packed FP32x2 pipe (FP32 / 16-bit storage only).
+template <int P, int N, int R, int MINB, bool PK>
+__global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashArgs A) {
+  using S = Store<P>;
+  using T = typename S::real;
+  using E = typename S::elem;
+  using namespace detail;
+  static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
+
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t site, grp;
+  A.div_groups.divmod(gid, site, grp);
+  if (site >= (uint32_t)A.geo.vh) return;
+  const uint32_t rhs0 = grp * R;
+  if (A.mask) {
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < R; r++) any |= A.mask[rhs0 + r] != 0;
+    if (!any) return;
+  }
+
+  uint32_t rest, xh, y, z, t;
+  A.geo.div_hx.divmod(site, rest, xh);
+  uint32_t rest2;
+  A.geo.div_y.divmod(rest, rest2, y);
+  A.geo.div_z.divmod(rest2, t, z);
+  const uint32_t hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
+  const uint32_t p = A.parity;
+  const uint32_t eo = (y + z + t) & 1u;
+  const T f = A.dagger ? (T)-1 : (T)1;
+  const uint32_t vh = A.geo.vh;
+  const uint32_t nrhs = A.nrhs;
+  const E* __restrict__ in = static_cast<const E*>(A.in);
+  const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
+  constexpr uint32_t NN = N * N;
+
+  HopAcc<T, N, R, PK> hacc;
+  hacc.zero();
+
+  // link offsets: forward links at (mu, p, site), backward at (mu, 1-p, nb)
+  const uint32_t lf = p * NN * vh + site;
+  const uint32_t lb = (1u - p) * NN * vh;
+  const uint32_t dmu = 2 * NN * vh;  // one direction's links
+  {  // X
+    const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+    const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+    hop_any<P, N, R, PK, 0, true>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
+  }
+  {  // Y
+    const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
+    const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
+    hop_any<P, N, R, PK, 1, true>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
+  }
+  {  // Z
+    const uint32_t pl = A.geo.plane;
+    const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
+    const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
+    hop_any<P, N, R, PK, 2, true>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
+  }
+  {  // T, with the optional antiperiodic sign
+    const uint32_t cb = A.geo.cube;
+    const bool top = t == Lt - 1, bot = t == 0;
+    const uint32_t nf = top ? site - (Lt - 1) * cb : site + cb;
+    const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
+    const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
+    const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
+    hop_any<P, N, R, PK, 3, true>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
+    hop_any<P, N, R, PK, 3, false>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
+  }
+
+  C2<T> acc[4][N][R];
+  hacc.to_rows(acc);
+
+  detail::store_out<P, N, R>(acc, A, site, rhs0);
 }
 
 // host-side launcher of one instantiation

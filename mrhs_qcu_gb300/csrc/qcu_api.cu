@@ -15,6 +15,7 @@
 
 #include "../../include/qcu.h"
 #include "../../include/qcu_gb300.h"
+#include "dslash_tma.h"
 #include "serve.h"
 #include "session.h"
 
@@ -405,17 +406,22 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     QCU_REQUIRE(count != nullptr && (shapes != nullptr || max_shapes == 0) && max_shapes >= 0,
                 QCU_ERR_INVALID_ARGUMENT, "qcuDslashKernels: bad output arrays");
     int n = 0;
+    auto put = [&](int R, int m, int pk, int st) {
+      if (n < max_shapes) {
+        shapes[4 * n] = R;
+        shapes[4 * n + 1] = m;
+        shapes[4 * n + 2] = pk;
+        shapes[4 * n + 3] = st;
+      }
+      n++;
+    };
     for (int R = 1; R <= 8; R++)
       for (int pk = 0; pk < 2; pk++)
         for (int m = 1; m <= 7; m++)
-          if (qcu::find_dslash(precision, nColors, R, m, pk)) {
-            if (n < max_shapes) {
-              shapes[3 * n] = R;
-              shapes[3 * n + 1] = m;
-              shapes[3 * n + 2] = pk;
-            }
-            n++;
-          }
+          if (qcu::find_dslash(precision, nColors, R, m, pk)) put(R, m, pk, 0);
+    int tr[32], ts[32];
+    const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
+    for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i]);
     *count = n;
   });
 }

@@ -6,6 +6,7 @@
 #include <sstream>
 
 #include "session.h"
+#include "dslash_tma.h"
 
 namespace qcu {
 
@@ -54,14 +55,13 @@ void Autotuner::load_file() {
   const char* path = getenv("QCU_TUNE_CACHE");
   if (!path) return;
   std::ifstream in(path);
-  std::string k;
-  int R, block, minb, pk;
-  while (in >> k >> R >> block >> minb >> pk) {
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::string k;
     DslashConfig c;
-    c.R = R;
-    c.block = block;
-    c.minb = minb;
-    c.pk = pk;
+    if (!(ls >> k >> c.R >> c.block >> c.minb >> c.pk)) continue;
+    if (!(ls >> c.tma >> c.rcta)) c.tma = c.rcta = 0;
     cache_[k] = c;
   }
 }
@@ -72,17 +72,22 @@ void Autotuner::save_file() {
   std::ofstream out(path);
   for (auto& kv : cache_)
     out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << " " << kv.second.pk
-        << "\n";
+        << " " << kv.second.tma << " " << kv.second.rcta << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
-  // QCU_DSLASH_CONFIG="R,block[,minb]" pins the kernel shape (profiling, sweeps)
+  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta]]]]" pins the kernel shape (profiling,
+  // sweeps); stages > 0 selects the TMA-staged kernel (block, reg_cap and packed are then ignored)
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    const int got = sscanf(f, "%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk);
-    if (got >= 2 && c.R >= 1 && nrhs % c.R == 0 && find_dslash(prec, N, c.R, c.minb, c.pk) && c.block >= 32 &&
-        c.block <= 256 && c.block % 32 == 0) {
+    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta);
+    const bool staged = got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 && find_tma(prec, N, c.R, c.tma);
+    const bool plain = got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
+                       find_dslash(prec, N, c.R, c.minb, c.pk) && c.block >= 32 && c.block <= 256 &&
+                       c.block % 32 == 0;
+    if (staged || plain) {
+      if (!staged) c.tma = c.rcta = 0;
       *found = true;
       return c;
     }
@@ -123,7 +128,7 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   }
   int opts[8];
   const int n = dslash_r_options(prec, N, opts, 8);
-  const int blocks[] = {64, 128, 256};
+  const int blocks[] = {32, 64, 128, 256};
   cudaEvent_t e0, e1;
   QCU_CHECK_CUDA(cudaEventCreate(&e0));
   QCU_CHECK_CUDA(cudaEventCreate(&e1));
@@ -154,6 +159,27 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
           best = c;
         }
       }
+    }
+  }
+  // the TMA-staged kernel, where these arguments fit it
+  int tr[16], ts[16];
+  const int nt = tma_options(prec, N, tr, ts, 16);
+  for (int i = 0; i < nt; i++) {
+    DslashConfig c;
+    c.R = tr[i];
+    c.tma = ts[i];
+    if (!tma_runs(A, prec, N, c)) continue;
+    launch_dslash(A, prec, N, c, st);  // warm-up
+    QCU_CHECK_CUDA(cudaEventRecord(e0, st));
+    const int reps = 3;
+    for (int k = 0; k < reps; k++) launch_dslash(A, prec, N, c, st);
+    QCU_CHECK_CUDA(cudaEventRecord(e1, st));
+    QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
     }
   }
   cudaEventDestroy(e0);
@@ -197,7 +223,11 @@ cudaStream_t Session::stream() {
   return own_stream_;
 }
 
-void Session::sync() { QCU_CHECK_CUDA(cudaStreamSynchronize(stream())); }
+void Session::sync() {
+  QCU_CHECK_CUDA(cudaStreamSynchronize(stream()));
+  QCU_REQUIRE(!tma_check_timeout(stream()), QCU_ERR_DEVICE_TIMEOUT,
+              "a staged dslash kernel timed out waiting for its copies (results invalid)");
+}
 
 void Session::load_gauge(const void* caller_gauge, int lex) {
   QCU_REQUIRE(caller_gauge != nullptr, QCU_ERR_INVALID_ARGUMENT, "gauge pointer is null");

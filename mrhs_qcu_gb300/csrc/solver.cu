@@ -559,7 +559,7 @@ std::vector<int> SlotEngine::step() {
   std::vector<int> act(n_), upd(n_);
   QCU_CHECK_CUDA(cudaMemcpyAsync(act.data(), S_.active, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
   QCU_CHECK_CUDA(cudaMemcpyAsync(upd.data(), S_.upd, sizeof(int) * n_, cudaMemcpyDeviceToHost, st_));
-  QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
+  s_.sync();
   std::vector<int> sel;
   for (int r = 0; r < n_; r++) {
     if (host_[r].phase != SlotState::ACTIVE) continue;

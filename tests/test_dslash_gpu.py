@@ -55,12 +55,14 @@ def test_colours_and_rhs_counts(cuda, qcu_lib, n, nrhs, prec):
 
 @pytest.mark.parametrize("prec", [2, 1, 0, 4])
 @pytest.mark.parametrize("n", [3, 4])
-def test_every_kernel_shape(cuda, qcu_lib, prec, n):
-    """Every compiled (R, min_blocks, packed) shape, pinned in turn, against
-    the oracle; the packed FP32x2 kernels bit-identical to the scalar kernel
-    of the same R (every lane performs the scalar FMA sequence)."""
+@pytest.mark.parametrize("L", [(4, 4, 4, 8), (12, 4, 6, 4)])
+def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
+    """Every compiled shape, pinned in turn, against the oracle: register
+    kernels (R, register cap, packed) and TMA-staged kernels (R, stages).  The
+    packed FP32x2 kernels and the staged kernels are bit-identical to the
+    scalar register kernel of the same R (they perform its FMA sequence)."""
     Q = qcu_lib
-    L, nrhs = (4, 4, 4, 8), 12
+    nrhs = 12
     g = S.random_gauge(L, n, seed=70 + n)
     psi = S.random_fermions(L, n, nrhs, seed=71)
     ref = {d: O.dslash(psi, g, L, d, d, True) for d in (0, 1)}
@@ -68,21 +70,21 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n):
     assert shapes
     outs = {}
     try:
-        for i, (R, minb, pk) in enumerate(shapes):
+        for i, (R, minb, pk, st) in enumerate(shapes):
             if nrhs % R:
                 continue
-            os.environ["QCU_DSLASH_CONFIG"] = "%d,%d,%d,%d" % (R, (64, 128, 256)[i % 3], minb, pk)
+            os.environ["QCU_DSLASH_CONFIG"] = "%d,%d,%d,%d,%d" % (R, (32, 64, 128, 256)[i % 4], minb, pk, st)
             for d in (0, 1):  # (parity 0, dagger 0) and (parity 1, dagger 1)
                 got = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
-                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, d)
-                outs[(R, minb, pk, d)] = got
+                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, d)
+                outs[(R, minb, pk, st, d)] = got
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
-    for (R, minb, pk, d), got in outs.items():
-        if pk:
-            for (r2, m2, p2, d2), other in outs.items():
-                if r2 == R and d2 == d and not p2:
-                    assert np.array_equal(got, other), (R, minb, m2, d)
+    for (R, minb, pk, st, d), got in outs.items():
+        if pk or st:
+            for (r2, m2, p2, s2, d2), other in outs.items():
+                if r2 == R and d2 == d and not p2 and not s2:
+                    assert np.array_equal(got, other), (R, minb, pk, st, m2, d)
 
 
 @pytest.mark.parametrize("prec", [0, 4])
