@@ -81,8 +81,9 @@ def profile_traffic():
             if line.strip() and not line.startswith("#"):
                 k, v = line.split(None, 1)
                 out[k] = v.strip()
-    if "dram_bytes_per_launch" in out:
-        out["dram_bytes_per_launch"] = float(out["dram_bytes_per_launch"])
+    for k in list(out):
+        if k.startswith("dram_bytes_per_launch"):
+            out[k] = float(out[k])
     return out
 
 
@@ -272,7 +273,7 @@ def run_gpu(args):
     nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
     Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
-    R, block, minb, pk = Q.tune_dslash(nrhs, prec)
+    R, block, minb, pk, stages = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
         Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
@@ -298,9 +299,10 @@ def run_gpu(args):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
-            "traffic": traffic.get("dram_bytes_per_launch")
+            "traffic": traffic.get("dram_bytes_per_launch_tma" if stages else "dram_bytes_per_launch_reg")
             if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1) else None,
-            "kernel": "wilson_mrhs_kernel<%s,N=3,R=%d,MINB=%d,PK=%d> block %d" % (pname, R, minb, pk, block),
+            "kernel": ("wilson_tma_kernel<%s,N=3,R=%d,stages=%d>" % (pname, R, stages)) if stages else
+                      ("wilson_mrhs_kernel<%s,N=3,R=%d,reg_cap=%d,PK=%d> block %d" % (pname, R, minb, pk, block)),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 

@@ -125,8 +125,9 @@ int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_
 /* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
  * Returns the chosen RHS-per-thread, block size, register-cap variant
  * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
- * 6 = 104) and whether the packed FP32x2 arithmetic variant was chosen. */
-int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed);
+ * 6 = 104), whether the packed FP32x2 arithmetic variant was chosen, and the
+ * ring depth of the TMA-staged kernel (0: the register kernel was chosen). */
+int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed, int *stages);
 
 /* No counterpart in the reference.  FMA throughput of the current GPU in
  * TFLOP/s (2 flop per FMA), precision QCU_DOUBLE_PRECISION or

@@ -131,7 +131,8 @@ def lib() -> ctypes.CDLL:
         "qcuEoToLex": ([P, P, I], I),
         "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
-        "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
+        "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
+                           ctypes.POINTER(I)], I),
         "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
         "qcuMeasureFmaRate": ([I, ctypes.POINTER(ctypes.c_double)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
@@ -303,10 +304,12 @@ def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:
 
 
 def tune_dslash(nrhs: int, precision: int):
-    R, B, M, K = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    """(R, block, reg_cap, packed, stages) of the tuned kernel; stages > 0:
+    the TMA-staged kernel."""
+    R, B, M, K, T = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M),
-                                  ctypes.byref(K)))
-    return R.value, B.value, M.value, K.value
+                                  ctypes.byref(K), ctypes.byref(T)))
+    return R.value, B.value, M.value, K.value, T.value
 
 
 def dslash_kernels(precision: int, n_colors: int = 3):

@@ -68,7 +68,10 @@ __device__ __forceinline__ uint64_t now_ns() {
 }
 
 // Wait until the phase with the given parity has completed; false after about
-// one second (then *err is set).
+// one second (then *err is set).  After the first poll the warp is suspended
+// in try_wait (suspend-time hint) until the phase completes or the hint runs
+// out, so waiting warps take no issue slots from working ones; the clock is
+// read every 16 polls.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
   uint32_t ok = 0;
   asm volatile(
@@ -78,14 +81,14 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
       : "memory");
   if (ok) return true;
   const uint64_t t0 = now_ns();
-  for (;;) {
+  for (uint32_t i = 1;; i++) {
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(1000000u)
         : "memory");
     if (ok) return true;
-    if (now_ns() - t0 > 1000000000ull) {
+    if ((i & 15u) == 0 && now_ns() - t0 > 1000000000ull) {
       atomicExch(err, 1);
       return false;
     }

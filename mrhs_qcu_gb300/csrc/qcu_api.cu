@@ -426,7 +426,8 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
   });
 }
 
-int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed) {
+int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed,
+                  int* stages) {
   return guarded([&] {
     Session& s = session();
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -457,6 +458,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (block) *block = c.block;
     if (min_blocks) *min_blocks = c.minb;
     if (packed) *packed = c.pk;
+    if (stages) *stages = c.tma;
   });
 }
 
