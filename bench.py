@@ -252,7 +252,7 @@ def run_gpu(args):
     world, rank, local, dist = dist_setup()
     torch.cuda.set_device(local)
     L = tuple(int(v) for v in args.lattice.split(","))
-    n, nrhs, prec = NC, args.nrhs, args.precision
+    n, nrhs, prec = args.ncolors, args.nrhs, args.precision
     pname = {0: "fp16", 1: "fp32", 2: "fp64", 4: "bf16"}[prec]
     vh = S.half_volume(L)
     g_dev, psi_dev = make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1 + rank)
@@ -300,9 +300,10 @@ def run_gpu(args):
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
             "traffic": traffic.get("dram_bytes_per_launch_tma" if stages else "dram_bytes_per_launch_reg")
-            if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1) else None,
-            "kernel": ("wilson_tma_kernel<%s,N=3,R=%d,stages=%d>" % (pname, R, stages)) if stages else
-                      ("wilson_mrhs_kernel<%s,N=3,R=%d,reg_cap=%d,PK=%d> block %d" % (pname, R, minb, pk, block)),
+            if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1 and n == NC) else None,
+            "kernel": ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
+                      ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
+                      ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d> block %d" % (pname, n, R, minb, pk, block)),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 
@@ -397,8 +398,8 @@ def run_gpu(args):
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
-            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), %s, nrhs=%d, %s, antiperiodic t"
-                                   % ("x".join(map(str, L)), nrhs, pname.upper()), "lattice": list(L), "nrhs": nrhs,
+            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(%d), %s, nrhs=%d, %s, antiperiodic t"
+                                   % (n, "x".join(map(str, L)), nrhs, pname.upper()), "lattice": list(L), "nrhs": nrhs,
                        "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
                        "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
             "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
@@ -479,13 +480,21 @@ def colors_bench(torch, Q, peak, fma):
     rows, solves = [], []
     for n in (4, 6, 8):
         g_dev, psi = make_inputs(torch, L, n, 64, seed_g=300 + n, seed_p=301)
-        for p, pname in ((1, "fp32"), (4, "bf16")):
+        # FP32: the autotuned CUDA-core kernel; BF16: CUDA cores (register kernel, R = 2) and the
+        # tensor-core (tcgen05) kernel, each pinned
+        for p, pname, kernel, pin in ((1, "fp32", "cuda_core", None), (4, "bf16", "cuda_core", "2,64,1,0"),
+                                      (4, "bf16", "tensor_core", "1,0,0,0,0,0,1")):
             for nr in (16, 32, 64):
-                ms_s, u = time_resident(torch, Q, L, n, nr, p, 10, 3, g_dev, psi)
+                if pin:
+                    os.environ["QCU_DSLASH_CONFIG"] = pin
+                try:
+                    ms_s, u = time_resident(torch, Q, L, n, nr, p, 10, 3, g_dev, psi)
+                finally:
+                    os.environ.pop("QCU_DSLASH_CONFIG", None)
                 rate = u / (ms_s * 1e-3)
                 gbs = bytes_per_site_rhs(p, n, nr) * rate / 1e9
                 tf = FLOPS_PER_SITE_RHS(n) * rate / 1e12
-                rows.append({"N": n, "precision": pname, "nrhs": nr, "ms": round(ms_s, 4),
+                rows.append({"N": n, "precision": pname, "kernel": kernel, "nrhs": nr, "ms": round(ms_s, 4),
                              "site_rhs_per_s": round(rate), "gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
                              "tflops": round(tf, 2),
                              "fp32_fma_frac": round(tf / fma["fp32_tflops"], 4) if fma else None})
@@ -516,8 +525,9 @@ def colors_bench(torch, Q, peak, fma):
                        "all_converged": all(prm.converged[r] for r in range(nr))})
         del g_dev, psi, b, x
         torch.cuda.empty_cache()
-    return {"workload": "16^3x32 SU(N) dslash (CUDA cores, FP32 arithmetic); BiCGStab kappa 0.11, FP32 inner, "
-                        "16 RHS (one 1e-4 smaller, one zero) to 1e-8",
+    return {"workload": "16^3x32 SU(N) dslash: FP32 storage on CUDA cores; BF16 storage on CUDA cores (FP32 "
+                        "arithmetic) and on the tensor cores (tcgen05, BF16 operands, FP32 accumulation); "
+                        "BiCGStab kappa 0.11, FP32 inner, 16 RHS (one 1e-4 smaller, one zero) to 1e-8",
             "dslash": rows, "bicgstab": solves}
 
 
@@ -651,6 +661,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--lattice", default="32,32,32,64", help="X,Y,Z,T of the headline workload")
     ap.add_argument("--nrhs", type=int, default=NRHS)
+    ap.add_argument("--ncolors", type=int, default=NC, help="N of SU(N) for the headline kernel (profiling)")
     ap.add_argument("--precision", type=int, default=1, help="0 fp16, 1 fp32, 2 fp64, 4 bf16")
     ap.add_argument("--profile", action="store_true",
                     help="headline kernel only (no e2e, sweep, CPU or solve legs), for ncu captures")

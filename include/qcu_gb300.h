@@ -126,7 +126,8 @@ int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_
  * Returns the chosen RHS-per-thread, block size, register-cap variant
  * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
  * 6 = 104), whether the packed FP32x2 arithmetic variant was chosen, and the
- * ring depth of the TMA-staged kernel (0: the register kernel was chosen). */
+ * ring depth of the TMA-staged kernel (0: the register kernel was chosen;
+ * -1: the tensor-core kernel). */
 int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed, int *stages);
 
 /* No counterpart in the reference.  FMA throughput of the current GPU in
@@ -138,8 +139,10 @@ int qcuMeasureFmaRate(int precision, double *tflops);
 /* The compiled dslash kernel shapes for (precision, nColors): *count
  * quadruples (RHS per thread, register-cap variant, packed, stages) are
  * available; the first max_shapes are written to shapes[4 * i .. 4 * i + 3].
- * stages > 0 is the TMA-staged kernel with that many ring buffers.  Any shape
- * can be pinned with QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages". */
+ * stages > 0 is the TMA-staged kernel with that many ring buffers, stages = -1
+ * the tensor-core (tcgen05) kernel.  Any shape can be pinned with
+ * QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages[,rcta,tensor]" (tensor = 1
+ * for the tensor-core kernel). */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 
 typedef struct QcuSolverParam_s {

@@ -3,6 +3,7 @@
 #include <mutex>
 
 #include "dslash.h"
+#include "dslash_tc.h"
 #include "dslash_tma.h"
 
 namespace qcu {
@@ -51,8 +52,31 @@ bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg) {
   return tma_plan(prec, N, A.geo, A.nrhs, cfg.R, cfg.tma, cfg.rcta, &T, &threads, &smem);
 }
 
+bool tc_runs(const DslashArgs& A, int prec, int N) {
+  TcDslashArgs T;
+  return find_tc(prec, N) && A.in_norm && A.out_norm && tc_plan(prec, N, A.geo, A.nrhs, &T);
+}
+
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
   DslashConfig cfg = cfg_in;
+  if (cfg.tc && tc_runs(A, prec, N)) {
+    DslashArgs B = A;
+    B.af = (float)A.a;
+    B.bf = (float)A.b;
+    find_tc(prec, N)(B, st);
+    QCU_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
+  if (cfg.tc) {  // arguments the tensor-core kernel cannot take: register kernel
+    cfg = DslashConfig{};
+    int opts[8];
+    const int n = dslash_r_options(prec, N, opts, 8);
+    for (int i = 0; i < n; i++)
+      if (A.nrhs % opts[i] == 0 && opts[i] <= 2) {
+        cfg.R = opts[i];
+        break;
+      }
+  }
   if (cfg.tma > 0) {
     if (tma_runs(A, prec, N, cfg)) {
       QCU_REQUIRE((int64_t)A.geo.vh * A.nrhs * prec_complex_bytes(prec) < (1ll << 32), QCU_ERR_INVALID_ARGUMENT,

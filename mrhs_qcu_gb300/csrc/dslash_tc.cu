@@ -1,0 +1,92 @@
+// Host side of the tensor-core dslash (see dslash_tc.h) and its instances.
+#include <algorithm>
+#include <map>
+#include <mutex>
+
+#include "dslash_tc.h"
+
+namespace qcu {
+namespace {
+
+std::map<int, TcLauncher>& registry() {
+  static std::map<int, TcLauncher> r;
+  return r;
+}
+std::mutex& registry_mutex() {
+  static std::mutex m;
+  return m;
+}
+
+struct RegisterTc {
+  RegisterTc() {
+    register_tc(PREC_BF16, 4, &launch_wilson_tc<4>);
+    register_tc(PREC_BF16, 5, &launch_wilson_tc<5>);
+    register_tc(PREC_BF16, 6, &launch_wilson_tc<6>);
+    register_tc(PREC_BF16, 7, &launch_wilson_tc<7>);
+    register_tc(PREC_BF16, 8, &launch_wilson_tc<8>);
+  }
+} register_tc_instances;
+
+}  // namespace
+
+bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, TcDslashArgs* T) {
+  if (prec != PREC_BF16 || N < 4 || N > 8 || nrhs < 1) return false;
+  // 32-bit element offsets into the field and the gauge
+  if ((int64_t)4 * N * geo.vh * nrhs >= (1ll << 32) || (int64_t)8 * N * N * geo.vh >= (1ll << 32)) return false;
+  int rt = 64;
+  while (nrhs % rt) rt--;
+  const int64_t ntiles = (int64_t)geo.vh * (nrhs / rt);
+  if (ntiles >= (1ll << 31)) return false;
+  T->rt = rt;
+  T->chunks = nrhs / rt;
+  T->ntiles = (int)ntiles;
+  return true;
+}
+
+// CTAs per SM from the kernel's registers and shared memory (the runtime's
+// occupancy query reports 1 for kernels that allocate tensor memory), capped
+// by the 512 tensor-memory columns at 32 per CTA.
+int tc_grid(const void* kernel, int ntiles) {
+  static std::mutex m;
+  static std::map<const void*, int> cache;
+  static int sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0;
+  std::lock_guard<std::mutex> lk(m);
+  if (!sms) {
+    int dev = 0;
+    QCU_CHECK_CUDA(cudaGetDevice(&dev));
+    QCU_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    QCU_CHECK_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+    QCU_CHECK_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+    QCU_CHECK_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
+    QCU_CHECK_CUDA(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
+  }
+  auto it = cache.find(kernel);
+  int occ = 0;
+  if (it == cache.end()) {
+    cudaFuncAttributes fa;
+    QCU_CHECK_CUDA(cudaFuncGetAttributes(&fa, kernel));
+    const int regs = (fa.numRegs + 7) / 8 * 8;  // allocation granularity
+    const int by_smem = smem_sm / (tc::kSmemBytes + (int)fa.sharedSizeBytes + reserved);
+    const int by_regs = regs_sm / (std::max(regs, 1) * 128);
+    const int by_thr = thr_sm / 128;
+    occ = std::min(std::min(by_smem, by_regs), std::min(by_thr, 16));
+    cache[kernel] = occ;
+  } else {
+    occ = it->second;
+  }
+  QCU_REQUIRE(occ >= 1, QCU_ERR_UNSUPPORTED, "tensor-core dslash does not fit on an SM");
+  return std::min(ntiles, occ * sms);
+}
+
+void register_tc(int prec, int N, TcLauncher fn) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  registry()[prec * 16 + N] = fn;
+}
+
+TcLauncher find_tc(int prec, int N) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  auto it = registry().find(prec * 16 + N);
+  return it == registry().end() ? nullptr : it->second;
+}
+
+}  // namespace qcu

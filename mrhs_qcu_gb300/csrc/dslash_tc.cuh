@@ -1,0 +1,345 @@
+// Tensor-core MRHS Wilson hop for SU(N), N = 4..8, BF16 storage (tcgen05).
+//
+// For one output site x and one hop (mu, +-), every RHS r and projected spin
+// row u in {0, 1} needs t_u(r) = W h_u(r), W = U_mu(x) or U_mu(x - mu)^dag, an
+// N x N complex link shared by all RHS.  Written as real matrices,
+//   D[m][n] += sum_k A[m][k] B[k][n],   m = 2 r + u,
+//   A[m][k]:  k < N: Re h_u(r)_k,  N <= k < 2N: Im h_u(r)_{k-N}   (zero padded to K = 16)
+//   B[k][n]:  [[Re W^T, Im W^T], [-Im W^T, Re W^T]] blocks        (zero padded to 16 x 16)
+// is one tcgen05.mma of M = 128 (64 RHS x 2 rows), N = 16, K = 16 per hop
+// for the upper spin rows, and a second one for the lower rows: the rows of
+// A' hold klo_u h_u at the lower row they feed (rows swapped for mu = x, y),
+// and B' = B times the +-i of the imaginary gamma rows (mu = x, z).  Both
+// accumulate over the eight hops in tensor memory (FP32, 2 x 16 columns of
+// 128 lanes), so the CUDA cores only project (h = psi_u + k psi_perm(u),
+// scaled by the neighbour's storage scale and the boundary sign), convert to
+// BF16 and write the operands; the N x N complex multiply runs on the tensor
+// pipe, with the link operand built once per hop and used by all RHS of the
+// tile.  The epilogue reads the accumulators back (tcgen05.ld), applies the
+// xpay / per-RHS a, and writes BF16 with per-(site, RHS) scales.
+//
+// CTA = 128 threads, thread m = 2 r + u owns row m (TMEM lane m).  Operands
+// are double buffered in shared memory; an mbarrier per buffer signals
+// (tcgen05.commit) when the MMAs reading it have finished.  Every wait is
+// bounded; a timeout sets *err, the CTA agrees to stop (__syncthreads_or),
+// waits once more (bounded) for its MMAs in flight, frees its tensor memory
+// and returns.  Tensor memory: 32 columns per CTA; the shared memory of a CTA
+// keeps at most 12 CTAs on an SM (384 of its 512 columns), so the allocation
+// never waits.
+#pragma once
+
+#include "dslash_kernel.cuh"
+#include "dslash_tma.cuh"
+
+namespace qcu {
+
+struct TcDslashArgs {
+  DslashArgs A;
+  int rt;      // RHS per tile (<= 64)
+  int chunks;  // nrhs / rt
+  int ntiles;  // vh * chunks
+  int* err;    // set to 1 when a wait times out
+};
+
+namespace tc {
+
+constexpr int kSetBytes = 9216;  // A 4096, A' 4096, B 512, B' 512
+constexpr int kSmemBytes = 2 * kSetBytes + 64;
+
+// shared-memory matrix descriptor: K-major, no swizzle; lbo = byte stride of
+// core matrices along K, sbo = along M (N for B); bits 46-48 = 0b001
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+         ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of element (row, k) in a K-major, no-swizzle operand with
+// K = 16: core matrices of 8 rows x 16 bytes, lbo = 128, sbo = 256
+__device__ __forceinline__ uint32_t kmaj_off(uint32_t row, uint32_t k) {
+  return (row >> 3) * 256u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's lane
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+}  // namespace tc
+
+template <int N>
+__global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ TcDslashArgs T) {
+  static_assert(N >= 2 && N <= 8, "K = 2N must fit one K = 16 MMA step");
+  using namespace detail;
+  using S = Store<PREC_BF16>;
+  using E = typename S::elem;
+  const DslashArgs& A = T.A;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * tc::kSetBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 2 * tc::kSetBytes + 16);
+  const uint32_t bar0 = tma::smem_u32(bars);
+  const uint32_t smem0 = tma::smem_u32(smem);
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  if (tid == 0) {
+    tma::mbar_init(bar0, 1);
+    tma::mbar_init(bar0 + 8, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tma::smem_u32(tmem_slot)),
+                 "r"(32u)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+  constexpr uint32_t idesc = tc::idesc_bf16(128, 16);
+
+  const int r = tid >> 1, u = tid & 1;
+  const bool row_live = r < T.rt;
+  const uint32_t vh = A.geo.vh, nrhs = A.nrhs, hx = A.geo.hx;
+  const uint32_t Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
+  const uint32_t p = A.parity;
+  const float f = A.dagger ? -1.f : 1.f;
+  const E* __restrict__ in = static_cast<const E*>(A.in);
+  const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
+  constexpr uint32_t NN = N * N;
+  const uint32_t cs = vh * nrhs;  // field component stride (elements)
+
+  // link operand: this thread writes elements (n, k0) and (n, k0 + 1) of the
+  // 16 x 16 (n, k) B and B' (one packed BF16 pair each)
+  const uint32_t bn = (uint32_t)tid >> 3, bk0 = ((uint32_t)tid & 7u) * 2u;
+  uint32_t boff_f[2], boff_b[2];  // link component * vh of the forward / backward link
+  bool bval[2], bnh = bn >= (uint32_t)N, bkh[2];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const uint32_t kk = bk0 + h;
+    bval[h] = bn < 2u * N && kk < 2u * N;
+    const uint32_t a = bn % N, bb = kk % N;
+    bkh[h] = kk >= (uint32_t)N;
+    boff_f[h] = (a * N + bb) * vh;
+    boff_b[h] = (bb * N + a) * vh;
+  }
+  const uint32_t boffs = tc::kmaj_off(bn, bk0);
+
+  uint32_t q = 0;  // hops issued so far (operand buffer = q & 1)
+  bool failed = false;
+  for (int tile = blockIdx.x; tile < T.ntiles && !failed; tile += gridDim.x) {
+    const uint32_t site = (uint32_t)(tile / T.chunks), chunk = (uint32_t)(tile % T.chunks);
+    const uint32_t rhs = chunk * (uint32_t)T.rt + (uint32_t)r;
+    uint32_t rest, xh, y, z, t, rest2;
+    A.geo.div_hx.divmod(site, rest, xh);
+    A.geo.div_y.divmod(rest, rest2, y);
+    A.geo.div_z.divmod(rest2, t, z);
+    const uint32_t eo = (y + z + t) & 1u;
+
+    for (int d = 0; d < 8; d++, q++) {
+      const int mu = d >> 1;
+      const bool fwd = (d & 1) == 0;
+      const uint32_t b = q & 1u;
+      // operand buffer b is free once the MMAs of hop q - 2 have completed
+      bool ok = true;
+      if (q >= 2) ok = tma::mbar_poll(bar0 + 8 * b, ((q >> 1) - 1) & 1u, T.err);
+      // neighbour site and link
+      uint32_t nb;
+      float bc = 1.f;
+      if (mu == 0) {
+        nb = fwd ? ((eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site)
+                 : ((eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site);
+      } else if (mu == 1) {
+        nb = fwd ? ((y == Ly - 1) ? site - (Ly - 1) * hx : site + hx) : ((y == 0) ? site + (Ly - 1) * hx : site - hx);
+      } else if (mu == 2) {
+        const uint32_t pl = A.geo.plane;
+        nb = fwd ? ((z == Lz - 1) ? site - (Lz - 1) * pl : site + pl) : ((z == 0) ? site + (Lz - 1) * pl : site - pl);
+      } else {
+        const uint32_t cb = A.geo.cube;
+        nb = fwd ? ((t == Lt - 1) ? site - (Lt - 1) * cb : site + cb) : ((t == 0) ? site + (Lt - 1) * cb : site - cb);
+        if (A.antiperiodic_t && (fwd ? t == Lt - 1 : t == 0)) bc = -1.f;
+      }
+      const uint32_t link_off = ((uint32_t)(2 * mu) + (fwd ? p : 1u - p)) * NN * vh + (fwd ? site : nb);
+      const bool imag = mu == 0 || mu == 2;
+      const float s = fwd ? -f : f;
+      unsigned char* set = smem + b * tc::kSetBytes;
+
+      if (ok && row_live) {
+        // projected row u of RHS rhs, scaled by bc * norm(nb, rhs)
+        const int up = (mu < 2) ? 3 - u : (u ^ 2);
+        const float scale = bc * __ldg(A.in_norm + (nb * nrhs + rhs));
+        const float ks = s * (float)gsign(mu, u) * scale;
+        const E* xp = in + ((uint32_t)(u * N) * cs + nb * nrhs + rhs);
+        const E* yp = in + ((uint32_t)(up * N) * cs + nb * nrhs + rhs);
+        float hr[N], hi[N];
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          const float2 x = S::to_c(__ldg(xp + (uint32_t)a * cs));
+          const float2 yv = S::to_c(__ldg(yp + (uint32_t)a * cs));
+          if (imag) {
+            hr[a] = fmaf(-ks, yv.y, scale * x.x);
+            hi[a] = fmaf(ks, yv.x, scale * x.y);
+          } else {
+            hr[a] = fmaf(ks, yv.x, scale * x.x);
+            hi[a] = fmaf(ks, yv.y, scale * x.y);
+          }
+        }
+        // A row tid; A' row (lower spin perm(u) - 2) = klo * h, klo = s * sign(mu, perm(u)) = +-1:
+        // the same BF16 values with the sign bits flipped when klo < 0
+        const uint32_t flip = (s * (float)gsign(mu, up) < 0.f) ? 0x80008000u : 0u;
+        const uint32_t row2 = (uint32_t)(2 * r + (up - 2));
+        uint32_t va[8], vb[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          float e[2];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            const int kk = 2 * j + h;
+            e[h] = kk < N ? hr[kk] : (kk < 2 * N ? hi[kk - N] : 0.f);
+          }
+          const __nv_bfloat162 v = __floats2bfloat162_rn(e[0], e[1]);
+          va[j] = *reinterpret_cast<const uint32_t*>(&v);
+          vb[j] = va[j] ^ flip;
+        }
+        *reinterpret_cast<uint4*>(set + tc::kmaj_off((uint32_t)tid, 0)) = make_uint4(va[0], va[1], va[2], va[3]);
+        *reinterpret_cast<uint4*>(set + tc::kmaj_off((uint32_t)tid, 8)) = make_uint4(va[4], va[5], va[6], va[7]);
+        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 0)) = make_uint4(vb[0], vb[1], vb[2], vb[3]);
+        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 8)) = make_uint4(vb[4], vb[5], vb[6], vb[7]);
+      }
+      if (ok) {
+        // B and B' (see the header comment): re t += wr re h - wi im h, im t += wi re h + wr im h;
+        // B' = B for real gamma rows, i t = (-im t, re t) for imaginary ones
+        float bv[2], bv2[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          bv[h] = bv2[h] = 0.f;
+          if (bval[h]) {
+            const float2 w = S::to_c(__ldg(gauge + (link_off + (fwd ? boff_f[h] : boff_b[h]))));
+            const float wr = w.x, wi = fwd ? w.y : -w.y;
+            bv[h] = bkh[h] ? (bnh ? wr : -wi) : (bnh ? wi : wr);
+            bv2[h] = !imag ? bv[h] : (bnh ? (bkh[h] ? -wi : wr) : -(bkh[h] ? wr : wi));
+          }
+        }
+        *reinterpret_cast<__nv_bfloat162*>(set + 8192 + boffs) = __floats2bfloat162_rn(bv[0], bv[1]);
+        *reinterpret_cast<__nv_bfloat162*>(set + 8704 + boffs) = __floats2bfloat162_rn(bv2[0], bv2[1]);
+      }
+      tc::fence_async_smem();
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      if (tid == 0) {
+        tc::fence_after();
+        const uint32_t base = smem0 + b * tc::kSetBytes;
+        const uint64_t da = tc::smem_desc(base, 128, 256), da2 = tc::smem_desc(base + 4096, 128, 256);
+        const uint64_t db = tc::smem_desc(base + 8192, 128, 256), db2 = tc::smem_desc(base + 8704, 128, 256);
+        tc::mma_bf16(tmem, da, db, idesc, d > 0);
+        tc::mma_bf16(tmem + 16, da2, db2, idesc, d > 0);
+        tc::commit(bar0 + 8 * b);
+      }
+    }
+    if (failed) break;
+
+    // all MMAs of this tile done (the commit of its last hop covers them)
+    const uint32_t ql = q - 1;
+    const bool ok = tma::mbar_poll(bar0 + 8 * (ql & 1u), (ql >> 1) & 1u, T.err);
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    tc::fence_after();
+    float up_v[16], lo_v[16];
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    tc::ld16(lane_addr, up_v);
+    tc::ld16(lane_addr + 16, lo_v);
+    tc::fence_before();
+
+    // epilogue: out spins u and 2 + u of RHS rhs at this site
+    float o[2][2 * N];
+#pragma unroll
+    for (int a = 0; a < N; a++) {
+      o[0][2 * a] = up_v[a];
+      o[0][2 * a + 1] = up_v[N + a];
+      o[1][2 * a] = lo_v[a];
+      o[1][2 * a + 1] = lo_v[N + a];
+    }
+    float mx = 0.f;
+    if (row_live) {
+      const float ca = A.a_rhs_f ? A.a_rhs_f[rhs] : A.af;
+      const E* __restrict__ xin = static_cast<const E*>(A.x);
+      const float xs = xin ? A.bf * A.x_norm[site * nrhs + rhs] : 0.f;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t sp = (uint32_t)(u + 2 * h);
+#pragma unroll
+        for (int a = 0; a < N; a++) {
+          float re = ca * o[h][2 * a], im = ca * o[h][2 * a + 1];
+          if (xin) {
+            const float2 xv = S::to_c(xin[(sp * N + a) * cs + site * nrhs + rhs]);
+            re = fmaf(xs, xv.x, re);
+            im = fmaf(xs, xv.y, im);
+          }
+          o[h][2 * a] = re;
+          o[h][2 * a + 1] = im;
+          mx = fmaxf(mx, fmaxf(fabsf(re), fabsf(im)));
+        }
+      }
+    }
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));  // the other two spins of this RHS (lane m ^ 1)
+    if (row_live && (!A.mask || A.mask[rhs] != 0)) {
+      const float inv = mx > 0.f ? 1.f / mx : 0.f;
+      E* __restrict__ out = static_cast<E*>(A.out);
+      if (u == 0) A.out_norm[site * nrhs + rhs] = mx;
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const uint32_t sp = (uint32_t)(u + 2 * h);
+#pragma unroll
+        for (int a = 0; a < N; a++)
+          out[(sp * N + a) * cs + site * nrhs + rhs] = S::from_c(make_float2(o[h][2 * a] * inv, o[h][2 * a + 1] * inv));
+      }
+    }
+  }
+
+  if (failed && tid == 0 && q > 0) {
+    // let the MMAs in flight finish before the tensor memory is released (bounded)
+    const uint32_t ql = q - 1;
+    tma::mbar_poll(bar0 + 8 * (ql & 1u), (ql >> 1) & 1u, T.err);
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32u) : "memory");
+}
+
+}  // namespace qcu

@@ -95,6 +95,27 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
   }
 }
 
+// The same bounded wait, polling with the non-blocking test_wait (no warp
+// suspension): for barriers that tcgen05.commit arrives on, where a short
+// wait is expected.
+__device__ __forceinline__ bool mbar_poll(uint32_t bar, uint32_t parity, int* err) {
+  uint64_t t0 = 0;
+  for (uint32_t i = 0;; i++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (i == 0) t0 = now_ns();
+    if ((i & 63u) == 63u && now_ns() - t0 > 1000000000ull) {
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+}
+
 // 2-D tiled TMA load into shared memory, completion counted on bar
 __device__ __forceinline__ void load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
   asm volatile(

@@ -15,6 +15,7 @@
 
 #include "../../include/qcu.h"
 #include "../../include/qcu_gb300.h"
+#include "dslash_tc.h"
 #include "dslash_tma.h"
 #include "serve.h"
 #include "session.h"
@@ -422,6 +423,7 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
     for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i]);
+    if (qcu::find_tc(precision, nColors)) put(1, 0, 0, -1);
     *count = n;
   });
 }
@@ -458,7 +460,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (block) *block = c.block;
     if (min_blocks) *min_blocks = c.minb;
     if (packed) *packed = c.pk;
-    if (stages) *stages = c.tma;
+    if (stages) *stages = c.tc ? -1 : c.tma;
   });
 }
 

@@ -6,6 +6,7 @@
 #include <sstream>
 
 #include "session.h"
+#include "dslash_tc.h"
 #include "dslash_tma.h"
 
 namespace qcu {
@@ -62,6 +63,7 @@ void Autotuner::load_file() {
     DslashConfig c;
     if (!(ls >> k >> c.R >> c.block >> c.minb >> c.pk)) continue;
     if (!(ls >> c.tma >> c.rcta)) c.tma = c.rcta = 0;
+    if (!(ls >> c.tc)) c.tc = 0;
     cache_[k] = c;
   }
 }
@@ -72,22 +74,26 @@ void Autotuner::save_file() {
   std::ofstream out(path);
   for (auto& kv : cache_)
     out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << " " << kv.second.pk
-        << " " << kv.second.tma << " " << kv.second.rcta << "\n";
+        << " " << kv.second.tma << " " << kv.second.rcta << " " << kv.second.tc << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
-  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta]]]]" pins the kernel shape (profiling,
-  // sweeps); stages > 0 selects the TMA-staged kernel (block, reg_cap and packed are then ignored)
+  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta[,tensor]]]]]" pins the kernel shape
+  // (profiling, sweeps); stages > 0 selects the TMA-staged kernel, tensor = 1 the tensor-core kernel
+  // (the other fields are then ignored)
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta);
-    const bool staged = got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 && find_tma(prec, N, c.R, c.tma);
-    const bool plain = got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
+    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc);
+    const bool tensor = got >= 7 && c.tc == 1 && find_tc(prec, N);
+    const bool staged = !tensor && got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 &&
+                        find_tma(prec, N, c.R, c.tma);
+    const bool plain = !tensor && got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
                        find_dslash(prec, N, c.R, c.minb, c.pk) && c.block >= 32 && c.block <= 256 &&
                        c.block % 32 == 0;
-    if (staged || plain) {
+    if (tensor || staged || plain) {
       if (!staged) c.tma = c.rcta = 0;
+      if (!tensor) c.tc = 0;
       *found = true;
       return c;
     }
@@ -169,6 +175,23 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
     c.R = tr[i];
     c.tma = ts[i];
     if (!tma_runs(A, prec, N, c)) continue;
+    launch_dslash(A, prec, N, c, st);  // warm-up
+    QCU_CHECK_CUDA(cudaEventRecord(e0, st));
+    const int reps = 3;
+    for (int k = 0; k < reps; k++) launch_dslash(A, prec, N, c, st);
+    QCU_CHECK_CUDA(cudaEventRecord(e1, st));
+    QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = c;
+    }
+  }
+  // the tensor-core kernel, where these arguments fit it
+  if (tc_runs(A, prec, N)) {
+    DslashConfig c;
+    c.tc = 1;
     launch_dslash(A, prec, N, c, st);  // warm-up
     QCU_CHECK_CUDA(cudaEventRecord(e0, st));
     const int reps = 3;

@@ -58,9 +58,11 @@ def test_colours_and_rhs_counts(cuda, qcu_lib, n, nrhs, prec):
 @pytest.mark.parametrize("L", [(4, 4, 4, 8), (12, 4, 6, 4)])
 def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     """Every compiled shape, pinned in turn, against the oracle: register
-    kernels (R, register cap, packed) and TMA-staged kernels (R, stages).  The
-    packed FP32x2 kernels and the staged kernels are bit-identical to the
-    scalar register kernel of the same R (they perform its FMA sequence)."""
+    kernels (R, register cap, packed), TMA-staged kernels (R, stages) and the
+    tensor-core kernel (BF16, N >= 4).  The packed FP32x2 kernels and the
+    staged kernels are bit-identical to the scalar register kernel of the same
+    R (they perform its FMA sequence); the tensor-core kernel rounds its
+    operands to BF16 and meets the 16-bit tolerance."""
     Q = qcu_lib
     nrhs = 12
     g = S.random_gauge(L, n, seed=70 + n)
@@ -73,7 +75,8 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
         for i, (R, minb, pk, st) in enumerate(shapes):
             if nrhs % R:
                 continue
-            os.environ["QCU_DSLASH_CONFIG"] = "%d,%d,%d,%d,%d" % (R, (32, 64, 128, 256)[i % 4], minb, pk, st)
+            os.environ["QCU_DSLASH_CONFIG"] = ("1,0,0,0,0,0,1" if st < 0 else
+                                               "%d,%d,%d,%d,%d" % (R, (32, 64, 128, 256)[i % 4], minb, pk, st))
             for d in (0, 1):  # (parity 0, dagger 0) and (parity 1, dagger 1)
                 got = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
                 assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, d)
@@ -81,10 +84,62 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
     for (R, minb, pk, st, d), got in outs.items():
-        if pk or st:
+        if pk or st > 0:
             for (r2, m2, p2, s2, d2), other in outs.items():
                 if r2 == R and d2 == d and not p2 and not s2:
                     assert np.array_equal(got, other), (R, minb, pk, st, m2, d)
+
+
+@pytest.mark.parametrize("n,nrhs", [(4, 16), (8, 16), (6, 24), (8, 64), (5, 128)])
+def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs):
+    """The tcgen05 kernel (BF16 storage and operands, FP32 accumulation in
+    tensor memory) against the FP64 oracle: both parities and dagger flags,
+    antiperiodic t, RHS counts that fill the 128 MMA rows, leave them partly
+    empty, or take two tiles."""
+    L = (4, 4, 4, 8)
+    g = S.random_gauge(L, n, seed=90 + n)
+    psi = S.random_fermions(L, n, nrhs, seed=91)
+    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,1"
+    try:
+        for parity, dag in ((0, 0), (1, 1), (1, 0)):
+            got = abi_dslash(cuda, qcu_lib, psi, g, L, parity, dag, 4, antiperiodic_t=True)
+            assert rel(got, O.dslash(psi, g, L, parity, dag, True)) < TOL[4], (parity, dag)
+        assert qcu_lib.tune_dslash(nrhs, 4)[4] == -1  # the pinned shape is the tensor-core kernel
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
+
+
+def test_tensor_core_xpay_resident(cuda, qcu_lib):
+    """xpay epilogue and per-site scales of the tensor-core kernel on resident fields."""
+    torch, Q = cuda, qcu_lib
+    L, n, nrhs = (4, 4, 4, 8), 4, 16
+    g = S.random_gauge(L, n, seed=95)
+    full = S.random_fermions(L, n, nrhs, seed=96, parities=2)
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(False)
+    dg = dev(torch, g)
+    Q.loadQcuGauge(dg.data_ptr())
+    db, nb = Q.field_bytes(4, nrhs)
+    bufs = [torch.empty(db // 8 + 2, dtype=torch.float64, device="cuda") for _ in range(3)]
+    norms = [torch.empty(nb // 4 + 4, dtype=torch.float32, device="cuda") for _ in range(3)]
+    src = [dev(torch, full[r]) for r in range(nrhs)]
+    ptrs = [x.data_ptr() for x in src]
+    Q.pack_fermions(bufs[0].data_ptr(), norms[0].data_ptr(), ptrs, Q.QCU_SRC_EO_FULL, 0, 4)
+    Q.pack_fermions(bufs[1].data_ptr(), norms[1].data_ptr(), ptrs, Q.QCU_SRC_EO_FULL, 1, 4)
+    a, b = 0.37, -1.25
+    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,1"
+    try:
+        Q.dslash_xpay_mrhs(bufs[2].data_ptr(), norms[2].data_ptr(), bufs[0].data_ptr(), norms[0].data_ptr(),
+                           bufs[1].data_ptr(), norms[1].data_ptr(), nrhs, 1, 0, 4, a, b)
+        outs = [torch.zeros((S.half_volume(L), 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
+        Q.unpack_fermions([o.data_ptr() for o in outs], bufs[2].data_ptr(), norms[2].data_ptr(),
+                          Q.QCU_SRC_EO_HALF, 1, 4)
+        Q.synchronize()
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
+    got = np.stack([o.cpu().numpy() for o in outs])
+    want = a * O.dslash(full[:, 0], g, L, 1, 0, False) + b * full[:, 1]
+    assert rel(got, want) < TOL[4]
 
 
 @pytest.mark.parametrize("prec", [0, 4])
