@@ -412,8 +412,8 @@ def run_gpu(args):
 
 def cpu_baseline(g_dev, psi_dev, L, n, budget_s=12.0):
     """FP64 OpenMP oracle dslash on the host cores, on a bounded sample of the
-    workload: the full 32^3x64 gauge, as many RHS of the benchmark field as fit
-    the time budget (one RHS per call)."""
+    workload: the full 32^3x64 gauge and the benchmark field's RHS, one RHS per
+    call, cycling over the RHS until about budget_s of host work is done."""
     from oracle import oracle as O
     g = g_dev.cpu().numpy()
     threads = O.num_threads()
@@ -423,15 +423,17 @@ def cpu_baseline(g_dev, psi_dev, L, n, budget_s=12.0):
     t0 = time.perf_counter()
     elapsed = 0.0
     r = 0
-    while elapsed < budget_s and r < psi_dev.shape[0]:
-        psi = psi_dev[r:r + 1].cpu().numpy()
+    host = [psi_dev[k:k + 1].cpu().numpy() for k in range(psi_dev.shape[0])]
+    while elapsed < budget_s:
+        psi = host[r % len(host)]
         t1 = time.perf_counter()
         O.dslash(psi, g, L, 0, 0, True)
         elapsed += time.perf_counter() - t1
         done += vh
         r += 1
     return {"value": done / elapsed, "unit": "site*RHS/s", "cores": threads, "kind": "port",
-            "sample": "%d RHS of the 32^3x64 SU(3) field, FP64, %.1f s" % (r, elapsed),
+            "sample": "%d single-RHS D_eo applications (cycling over the %d RHS) of the 32^3x64 SU(3) "
+                      "workload, FP64, %.1f s" % (r, len(host), elapsed),
             "wall_s": round(time.perf_counter() - t0, 2)}
 
 

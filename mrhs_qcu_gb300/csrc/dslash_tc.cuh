@@ -4,8 +4,8 @@
 // row u in {0, 1} needs t_u(r) = W h_u(r), W = U_mu(x) or U_mu(x - mu)^dag, an
 // N x N complex link shared by all RHS.  Written as real matrices,
 //   D[m][n] += sum_k A[m][k] B[k][n],   m = 2 r + u,
-//   A[m][k]:  k < N: Re h_u(r)_k,  N <= k < 2N: Im h_u(r)_{k-N}   (zero padded to K = 16)
-//   B[k][n]:  [[Re W^T, Im W^T], [-Im W^T, Re W^T]] blocks        (zero padded to 16 x 16)
+//   A[m][2b + c] = (Re, Im)_c of h_u(r)_b            (one packed BF16 pair per colour; K padded to 16)
+//   B[2b + c][2a + c'] = the 2x2 real block of W_ab: [[Re W_ab, Im W_ab], [-Im W_ab, Re W_ab]]
 // is one tcgen05.mma of M = 128 (64 RHS x 2 rows), N = 16, K = 16 per hop
 // for the upper spin rows, and a second one for the lower rows: the rows of
 // A' hold klo_u h_u at the lower row they feed (rows swapped for mu = x, y),
@@ -27,6 +27,8 @@
 // keeps at most 12 CTAs on an SM (384 of its 512 columns), so the allocation
 // never waits.
 #pragma once
+
+#include <type_traits>
 
 #include "dslash_kernel.cuh"
 #include "dslash_tma.cuh"
@@ -141,21 +143,13 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
   constexpr uint32_t NN = N * N;
   const uint32_t cs = vh * nrhs;  // field component stride (elements)
 
-  // link operand: this thread writes elements (n, k0) and (n, k0 + 1) of the
-  // 16 x 16 (n, k) B and B' (one packed BF16 pair each)
-  const uint32_t bn = (uint32_t)tid >> 3, bk0 = ((uint32_t)tid & 7u) * 2u;
-  uint32_t boff_f[2], boff_b[2];  // link component * vh of the forward / backward link
-  bool bval[2], bnh = bn >= (uint32_t)N, bkh[2];
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    const uint32_t kk = bk0 + h;
-    bval[h] = bn < 2u * N && kk < 2u * N;
-    const uint32_t a = bn % N, bb = kk % N;
-    bkh[h] = kk >= (uint32_t)N;
-    boff_f[h] = (a * N + bb) * vh;
-    boff_b[h] = (bb * N + a) * vh;
-  }
-  const uint32_t boffs = tc::kmaj_off(bn, bk0);
+  // link operand: this thread writes elements (n, 2b) and (n, 2b + 1) of the
+  // 16 x 16 (n, k) B and B' (one packed BF16 pair each), n = 2a + c (colour a
+  // of t, c = Re / Im), k = 2b + c' (colour b of h): both come from W_ab
+  const uint32_t bn = (uint32_t)tid >> 3, bb = (uint32_t)tid & 7u, ba = bn >> 1;
+  const bool bim = (bn & 1u) != 0, bval = ba < (uint32_t)N && bb < (uint32_t)N;
+  const uint32_t boff_f = (ba * N + bb) * vh, boff_b = (bb * N + ba) * vh;  // W = U_ab, or conj(U_ba)
+  const uint32_t boffs = tc::kmaj_off(bn, 2 * bb);
 
   uint32_t q = 0;  // hops issued so far (operand buffer = q & 1)
   bool failed = false;
@@ -168,22 +162,25 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
     A.geo.div_z.divmod(rest2, t, z);
     const uint32_t eo = (y + z + t) & 1u;
 
-    for (int d = 0; d < 8; d++, q++) {
-      const int mu = d >> 1;
-      const bool fwd = (d & 1) == 0;
+    // hop D (mu = D / 2, forward for even D), all choices of the hop known at
+    // compile time; returns false when the CTA stops after a timeout
+    auto hop = [&](auto dc) -> bool {
+      constexpr int D = decltype(dc)::value;
+      constexpr int mu = D >> 1;
+      constexpr bool fwd = (D & 1) == 0;
+      constexpr bool imag = mu == 0 || mu == 2;
       const uint32_t b = q & 1u;
       // operand buffer b is free once the MMAs of hop q - 2 have completed
       bool ok = true;
       if (q >= 2) ok = tma::mbar_poll(bar0 + 8 * b, ((q >> 1) - 1) & 1u, T.err);
-      // neighbour site and link
       uint32_t nb;
       float bc = 1.f;
-      if (mu == 0) {
+      if constexpr (mu == 0) {
         nb = fwd ? ((eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site)
                  : ((eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site);
-      } else if (mu == 1) {
+      } else if constexpr (mu == 1) {
         nb = fwd ? ((y == Ly - 1) ? site - (Ly - 1) * hx : site + hx) : ((y == 0) ? site + (Ly - 1) * hx : site - hx);
-      } else if (mu == 2) {
+      } else if constexpr (mu == 2) {
         const uint32_t pl = A.geo.plane;
         nb = fwd ? ((z == Lz - 1) ? site - (Lz - 1) * pl : site + pl) : ((z == 0) ? site + (Lz - 1) * pl : site - pl);
       } else {
@@ -191,85 +188,81 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
         nb = fwd ? ((t == Lt - 1) ? site - (Lt - 1) * cb : site + cb) : ((t == 0) ? site + (Lt - 1) * cb : site - cb);
         if (A.antiperiodic_t && (fwd ? t == Lt - 1 : t == 0)) bc = -1.f;
       }
-      const uint32_t link_off = ((uint32_t)(2 * mu) + (fwd ? p : 1u - p)) * NN * vh + (fwd ? site : nb);
-      const bool imag = mu == 0 || mu == 2;
       const float s = fwd ? -f : f;
       unsigned char* set = smem + b * tc::kSetBytes;
 
       if (ok && row_live) {
-        // projected row u of RHS rhs, scaled by bc * norm(nb, rhs)
+        // projected row u of RHS rhs, scaled by bc * norm(nb, rhs); A row word c = (Re h_c, Im h_c)
         const int up = (mu < 2) ? 3 - u : (u ^ 2);
         const float scale = bc * __ldg(A.in_norm + (nb * nrhs + rhs));
         const float ks = s * (float)gsign(mu, u) * scale;
         const E* xp = in + ((uint32_t)(u * N) * cs + nb * nrhs + rhs);
         const E* yp = in + ((uint32_t)(up * N) * cs + nb * nrhs + rhs);
-        float hr[N], hi[N];
+        uint32_t va[8];
 #pragma unroll
-        for (int a = 0; a < N; a++) {
-          const float2 x = S::to_c(__ldg(xp + (uint32_t)a * cs));
-          const float2 yv = S::to_c(__ldg(yp + (uint32_t)a * cs));
-          if (imag) {
-            hr[a] = fmaf(-ks, yv.y, scale * x.x);
-            hi[a] = fmaf(ks, yv.x, scale * x.y);
+        for (int a = 0; a < 8; a++) {
+          if (a < N) {
+            const float2 x = S::to_c(__ldg(xp + (uint32_t)a * cs));
+            const float2 yv = S::to_c(__ldg(yp + (uint32_t)a * cs));
+            float hr, hi;
+            if constexpr (imag) {
+              hr = fmaf(-ks, yv.y, scale * x.x);
+              hi = fmaf(ks, yv.x, scale * x.y);
+            } else {
+              hr = fmaf(ks, yv.x, scale * x.x);
+              hi = fmaf(ks, yv.y, scale * x.y);
+            }
+            const __nv_bfloat162 v = __floats2bfloat162_rn(hr, hi);
+            va[a] = *reinterpret_cast<const uint32_t*>(&v);
           } else {
-            hr[a] = fmaf(ks, yv.x, scale * x.x);
-            hi[a] = fmaf(ks, yv.y, scale * x.y);
+            va[a] = 0u;
           }
         }
-        // A row tid; A' row (lower spin perm(u) - 2) = klo * h, klo = s * sign(mu, perm(u)) = +-1:
-        // the same BF16 values with the sign bits flipped when klo < 0
+        // A' row (lower spin perm(u) - 2) = klo * h, klo = s * sign(mu, perm(u)) = +-1: sign bits flipped
         const uint32_t flip = (s * (float)gsign(mu, up) < 0.f) ? 0x80008000u : 0u;
         const uint32_t row2 = (uint32_t)(2 * r + (up - 2));
-        uint32_t va[8], vb[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          float e[2];
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            const int kk = 2 * j + h;
-            e[h] = kk < N ? hr[kk] : (kk < 2 * N ? hi[kk - N] : 0.f);
-          }
-          const __nv_bfloat162 v = __floats2bfloat162_rn(e[0], e[1]);
-          va[j] = *reinterpret_cast<const uint32_t*>(&v);
-          vb[j] = va[j] ^ flip;
-        }
         *reinterpret_cast<uint4*>(set + tc::kmaj_off((uint32_t)tid, 0)) = make_uint4(va[0], va[1], va[2], va[3]);
         *reinterpret_cast<uint4*>(set + tc::kmaj_off((uint32_t)tid, 8)) = make_uint4(va[4], va[5], va[6], va[7]);
-        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 0)) = make_uint4(vb[0], vb[1], vb[2], vb[3]);
-        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 8)) = make_uint4(vb[4], vb[5], vb[6], vb[7]);
+        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 0)) =
+            make_uint4(va[0] ^ flip, va[1] ^ flip, va[2] ^ flip, va[3] ^ flip);
+        *reinterpret_cast<uint4*>(set + 4096 + tc::kmaj_off(row2, 8)) =
+            make_uint4(va[4] ^ flip, va[5] ^ flip, va[6] ^ flip, va[7] ^ flip);
       }
       if (ok) {
-        // B and B' (see the header comment): re t += wr re h - wi im h, im t += wi re h + wr im h;
-        // B' = B for real gamma rows, i t = (-im t, re t) for imaginary ones
-        float bv[2], bv2[2];
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-          bv[h] = bv2[h] = 0.f;
-          if (bval[h]) {
-            const float2 w = S::to_c(__ldg(gauge + (link_off + (fwd ? boff_f[h] : boff_b[h]))));
-            const float wr = w.x, wi = fwd ? w.y : -w.y;
-            bv[h] = bkh[h] ? (bnh ? wr : -wi) : (bnh ? wi : wr);
-            bv2[h] = !imag ? bv[h] : (bnh ? (bkh[h] ? -wi : wr) : -(bkh[h] ? wr : wi));
-          }
+        // B: re t_a = sum_b wr re h_b - wi im h_b, im t_a = sum_b wi re h_b + wr im h_b;
+        // B' = B for real gamma rows, (re, im) of i t = (-im t, re t) for imaginary ones
+        float2 bv = make_float2(0.f, 0.f), bv2 = make_float2(0.f, 0.f);
+        if (bval) {
+          const uint32_t link_off = ((uint32_t)(2 * mu) + (fwd ? p : 1u - p)) * NN * vh + (fwd ? site : nb);
+          const float2 w = S::to_c(__ldg(gauge + (link_off + (fwd ? boff_f : boff_b))));
+          const float wr = w.x, wi = fwd ? w.y : -w.y;
+          bv = bim ? make_float2(wi, wr) : make_float2(wr, -wi);
+          if constexpr (imag)
+            bv2 = bim ? make_float2(wr, -wi) : make_float2(-wi, -wr);
+          else
+            bv2 = bv;
         }
-        *reinterpret_cast<__nv_bfloat162*>(set + 8192 + boffs) = __floats2bfloat162_rn(bv[0], bv[1]);
-        *reinterpret_cast<__nv_bfloat162*>(set + 8704 + boffs) = __floats2bfloat162_rn(bv2[0], bv2[1]);
+        *reinterpret_cast<__nv_bfloat162*>(set + 8192 + boffs) = __floats2bfloat162_rn(bv.x, bv.y);
+        *reinterpret_cast<__nv_bfloat162*>(set + 8704 + boffs) = __floats2bfloat162_rn(bv2.x, bv2.y);
       }
       tc::fence_async_smem();
-      if (__syncthreads_or(!ok)) {
-        failed = true;
-        break;
-      }
+      if (__syncthreads_or(!ok)) return false;
       if (tid == 0) {
         tc::fence_after();
         const uint32_t base = smem0 + b * tc::kSetBytes;
         const uint64_t da = tc::smem_desc(base, 128, 256), da2 = tc::smem_desc(base + 4096, 128, 256);
         const uint64_t db = tc::smem_desc(base + 8192, 128, 256), db2 = tc::smem_desc(base + 8704, 128, 256);
-        tc::mma_bf16(tmem, da, db, idesc, d > 0);
-        tc::mma_bf16(tmem + 16, da2, db2, idesc, d > 0);
+        tc::mma_bf16(tmem, da, db, idesc, D > 0);
+        tc::mma_bf16(tmem + 16, da2, db2, idesc, D > 0);
         tc::commit(bar0 + 8 * b);
       }
-    }
+      q++;
+      return true;
+    };
+    failed = !(hop(std::integral_constant<int, 0>{}) && hop(std::integral_constant<int, 1>{}) &&
+               hop(std::integral_constant<int, 2>{}) && hop(std::integral_constant<int, 3>{}) &&
+               hop(std::integral_constant<int, 4>{}) && hop(std::integral_constant<int, 5>{}) &&
+               hop(std::integral_constant<int, 6>{}) && hop(std::integral_constant<int, 7>{}));
     if (failed) break;
 
     // all MMAs of this tile done (the commit of its last hop covers them)
@@ -287,13 +280,11 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
     tc::fence_before();
 
     // epilogue: out spins u and 2 + u of RHS rhs at this site
-    float o[2][2 * N];
+    float o[2][2 * N];  // D column 2a + c = (Re, Im) of colour a
 #pragma unroll
-    for (int a = 0; a < N; a++) {
-      o[0][2 * a] = up_v[a];
-      o[0][2 * a + 1] = up_v[N + a];
-      o[1][2 * a] = lo_v[a];
-      o[1][2 * a + 1] = lo_v[N + a];
+    for (int a = 0; a < 2 * N; a++) {
+      o[0][a] = up_v[a];
+      o[1][a] = lo_v[a];
     }
     float mx = 0.f;
     if (row_live) {

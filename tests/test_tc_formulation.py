@@ -1,8 +1,9 @@
 """CPU check of the tensor-core dslash formulation (csrc/dslash_tc.cuh): the
 real-matrix operands A, A', B, B' built the way the kernel builds them (rows
-m = 2r + u, K = Re/Im of the input colours, N = Re/Im of the output colours,
-zero padded to 16; A' rows swapped and signed, B' times +-i), multiplied and
-accumulated over the eight hops in FP64, reproduce the oracle's hop term."""
+m = 2r + u; K index 2b + c = Re / Im of input colour b; N index 2a + c = Re /
+Im of output colour a; zero padded to 16; A' rows swapped and signed, B'
+times +-i), multiplied and accumulated over the eight hops in FP64,
+reproduce the oracle's hop term."""
 import numpy as np
 import pytest
 
@@ -63,24 +64,27 @@ def tc_hop(psi, g, L, p, dagger, antiperiodic):
                     h = ((x.real - k * yv.imag) + 1j * (x.imag + k * yv.real)) if imag else x + k * yv
                     h = h * bc
                     row = np.zeros(16)
-                    row[:N], row[N:2 * N] = h.real, h.imag
+                    row[0:2 * N:2], row[1:2 * N:2] = h.real, h.imag
                     a_up[2 * r + u] = row
                     a_lo[2 * r + (up - 2)] = s * gsign(mu, up) * row
             b = np.zeros((16, 16))
-            b2 = np.zeros((16, 16))
-            for n in range(2 * N):
-                for kk in range(2 * N):
-                    a, bb, nh, kh = n % N, kk % N, n >= N, kk >= N
+            for a in range(N):
+                for bb in range(N):
                     w = w_link[a, bb] if fwd else np.conj(w_link[bb, a])
                     wr, wi = w.real, w.imag
-                    b[kk, n] = (wr if nh else -wi) if kh else (wi if nh else wr)
-                    b2[kk, n] = b[kk, n] if not imag else ((-wi if kh else wr) if nh else -(wr if kh else wi))
+                    # re t_a += wr re h_b - wi im h_b; im t_a += wi re h_b + wr im h_b
+                    b[2 * bb, 2 * a], b[2 * bb + 1, 2 * a] = wr, -wi
+                    b[2 * bb, 2 * a + 1], b[2 * bb + 1, 2 * a + 1] = wi, wr
+            # B' = B for real gamma rows; i t = (-im t, re t) for imaginary ones
+            b2 = b.copy()
+            if imag:
+                b2[:, 0:2 * N:2], b2[:, 1:2 * N:2] = -b[:, 1:2 * N:2], b[:, 0:2 * N:2]
             d_up += a_up @ b
             d_lo += a_lo @ b2
         for r in range(nrhs):
             for u in range(2):
-                out[r, site, u] = d_up[2 * r + u, :N] + 1j * d_up[2 * r + u, N:2 * N]
-                out[r, site, 2 + u] = d_lo[2 * r + u, :N] + 1j * d_lo[2 * r + u, N:2 * N]
+                out[r, site, u] = d_up[2 * r + u, 0:2 * N:2] + 1j * d_up[2 * r + u, 1:2 * N:2]
+                out[r, site, 2 + u] = d_lo[2 * r + u, 0:2 * N:2] + 1j * d_lo[2 * r + u, 1:2 * N:2]
     return out
 
 
