@@ -273,7 +273,7 @@ def run_gpu(args):
     nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
     Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
-    R, block, minb, pk, stages = Q.tune_dslash(nrhs, prec)
+    R, block, minb, pk, stages, recon = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
         Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
@@ -299,11 +299,14 @@ def run_gpu(args):
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
-            "traffic": traffic.get("dram_bytes_per_launch_tma" if stages else "dram_bytes_per_launch_reg")
+            # measured DRAM bytes of the kernel the tuner picked (profiles/dslash_traffic.txt)
+            "traffic": traffic.get("dram_bytes_per_launch_tma" if stages > 0 else
+                                   "dram_bytes_per_launch_rc" if recon else "dram_bytes_per_launch_reg")
             if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1 and n == NC) else None,
             "kernel": ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
                       ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
-                      ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d> block %d" % (pname, n, R, minb, pk, block)),
+                      ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
+                       % (pname, n, R, minb, pk, recon, block)),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     Q.set_stream(None)
 

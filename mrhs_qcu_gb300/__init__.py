@@ -132,7 +132,7 @@ def lib() -> ctypes.CDLL:
         "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
         "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
-                           ctypes.POINTER(I)], I),
+                           ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
         "qcuMeasureFmaRate": ([I, ctypes.POINTER(ctypes.c_double)], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
@@ -304,21 +304,23 @@ def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:
 
 
 def tune_dslash(nrhs: int, precision: int):
-    """(R, block, reg_cap, packed, stages) of the tuned kernel; stages > 0:
-    the TMA-staged kernel."""
-    R, B, M, K, T = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    """(R, block, reg_cap, packed, stages, recon) of the tuned kernel; stages
+    > 0: the TMA-staged kernel, -1: the tensor-core kernel; recon: two-row
+    SU(3) links."""
+    R, B, M, K, T, C = (ctypes.c_int() for _ in range(6))
     _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M),
-                                  ctypes.byref(K), ctypes.byref(T)))
-    return R.value, B.value, M.value, K.value, T.value
+                                  ctypes.byref(K), ctypes.byref(T), ctypes.byref(C)))
+    return R.value, B.value, M.value, K.value, T.value, C.value
 
 
 def dslash_kernels(precision: int, n_colors: int = 3):
-    """Compiled dslash kernel shapes [(R, reg_cap, packed, stages), ...];
-    stages > 0 is the TMA-staged kernel."""
-    arr = (ctypes.c_int * (4 * 64))()
+    """Compiled dslash kernel shapes [(R, reg_cap, packed, stages, recon), ...];
+    stages > 0: the TMA-staged kernel, -1: the tensor-core kernel; recon: two-row
+    SU(3) links."""
+    arr = (ctypes.c_int * (5 * 64))()
     cnt = ctypes.c_int()
     _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
-    return [tuple(arr[4 * i:4 * i + 4]) for i in range(min(cnt.value, 64))]
+    return [tuple(arr[5 * i:5 * i + 5]) for i in range(min(cnt.value, 64))]
 
 
 def measure_fma_rate(precision: int) -> float:

@@ -16,17 +16,23 @@ std::mutex& registry_mutex() {
   static std::mutex m;
   return m;
 }
-int key(int prec, int N, int R, int minb, int pk) { return (((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk; }
+int key(int prec, int N, int R, int minb, int pk, int rc) {
+  return ((((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk) * 2 + rc;
+}
 }  // namespace
 
-void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn) {
+void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[key(prec, N, R, minb, pk)] = fn;
+  registry()[key(prec, N, R, minb, pk, rc)] = fn;
 }
 
-DslashLauncher find_dslash(int prec, int N, int R, int minb, int pk) {
+void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn) {
+  register_dslash(prec, N, R, minb, pk, 0, fn);
+}
+
+DslashLauncher find_dslash(int prec, int N, int R, int minb, int pk, int rc) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find(key(prec, N, R, minb, pk));
+  auto it = registry().find(key(prec, N, R, minb, pk, rc));
   return it == registry().end() ? nullptr : it->second;
 }
 
@@ -37,10 +43,10 @@ int dslash_r_options(int prec, int N, int* out, int max) {
   return n;
 }
 
-int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max) {
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc) {
   int n = 0;
   for (int m = 1; m <= 7 && n < max; m++)
-    if (find_dslash(prec, N, R, m, pk)) out[n++] = m;
+    if (find_dslash(prec, N, R, m, pk, rc)) out[n++] = m;
   return n;
 }
 
@@ -98,7 +104,12 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
         break;
       }
   }
-  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk);
+  if (cfg.rc && (!A.gauge12 || !find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 1))) {
+    // no two-row gauge for this field (not SU(3) to rounding): the full links
+    cfg.rc = 0;
+    if (!find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 0)) cfg.minb = 1, cfg.pk = 0;
+  }
+  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, cfg.rc);
   QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
               std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +
                   ", R=" + std::to_string(cfg.R) + ", minb=" + std::to_string(cfg.minb) +

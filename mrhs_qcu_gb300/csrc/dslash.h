@@ -15,13 +15,15 @@ using DslashLauncher = void (*)(const DslashArgs&, int block, cudaStream_t);
 // registry filled by the instantiation units (dslash_inst_*.cu); minb is the
 // register-cap variant of the kernel (RegCap in dslash_kernel.cuh)
 // pk selects the packed FP32x2 arithmetic variant
-DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0);
+// rc selects the SU(3) variant that reads two-row links and reconstructs the third
+DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0, int rc = 0);
 void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn);
+void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn);
 
 // RHS-per-thread values compiled for (prec, N), largest first
 int dslash_r_options(int prec, int N, int* out, int max);
 // register-cap variants compiled for (prec, N, R, pk), ascending
-int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max);
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc = 0);
 
 struct DslashConfig {
   int R = 1;
@@ -31,6 +33,7 @@ struct DslashConfig {
   int tma = 0;   // > 0: the TMA-staged kernel (dslash_tma.cuh) with this many ring stages
   int rcta = 0;  // its RHS per tile (0: the largest that fits)
   int tc = 0;    // 1: the tensor-core kernel (dslash_tc.cuh)
+  int rc = 0;    // 1: SU(3) two-row links with the third row reconstructed (register kernel)
 };
 
 // whether the staged kernel of cfg can run these arguments

@@ -28,6 +28,7 @@ namespace qcu {
 
 struct DslashArgs {
   const void* gauge;     // [4][2][N*N][Vh] complex<P>
+  const void* gauge12 = nullptr;  // SU(3): [4][2][6][Vh], the first two rows (or nullptr)
   const void* in;        // MRHS field, parity 1 - parity
   const float* in_norm;  // [Vh][nrhs] (16-bit storage only)
   void* out;             // MRHS field, output parity
@@ -164,7 +165,7 @@ __device__ __forceinline__ void load_norms(const float* p, float (&nrm)[R]) {
 //   klo  = s * sign(lo) * bc * scale_r   the reconstructed lower rows
 // Offsets are 32-bit element indices into the field / gauge arrays (the host
 // checks that every array has fewer than 2^32 elements).
-template <int P, int N, int R, int MU, bool FWD>
+template <int P, int N, int R, int MU, bool FWD, bool RC = false>
 __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R], const DslashArgs& A,
                                    const typename Store<P>::elem* __restrict__ in,
                                    const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
@@ -230,6 +231,27 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
   const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);
   const T klo0 = s * (T)gsign(MU, u0p), klo1 = s * (T)gsign(MU, u1p);
+  // SU(3) two-row links: row 2 = conj(row 0 x row 1), reconstructed in the arithmetic precision
+  C2<T> ul[RC ? 3 : 1][RC ? 3 : 1];
+  if constexpr (RC) {
+    static_assert(N == 3, "link reconstruction is SU(3) only");
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+        const auto v = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)(a * 3 + b) * ls_bytes)));
+        ul[a][b].x = (T)v.x;
+        ul[a][b].y = (T)v.y;
+      }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int k = (j + 1) % 3, l = (j + 2) % 3;
+      ul[2][j].x = (ul[0][k].x * ul[1][l].x - ul[0][k].y * ul[1][l].y) -
+                   (ul[0][l].x * ul[1][k].x - ul[0][l].y * ul[1][k].y);
+      ul[2][j].y = -((ul[0][k].x * ul[1][l].y + ul[0][k].y * ul[1][l].x) -
+                     (ul[0][l].x * ul[1][k].y + ul[0][l].y * ul[1][k].x));
+    }
+  }
 #pragma unroll
   for (int a = 0; a < N; a++) {
     C2<T> t[2][R];
@@ -240,10 +262,17 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 #pragma unroll
     for (int b = 0; b < N; b++) {
       // forward uses U[a][b]; backward uses conj(U[b][a])
-      const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
-      auto uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp * ls_bytes)));
-      const T ur = (T)uc.x;
-      const T ui = FWD ? (T)uc.y : -(T)uc.y;
+      T ur, ui;
+      if constexpr (RC) {
+        const C2<T> uc = FWD ? ul[a][b] : ul[b][a];
+        ur = uc.x;
+        ui = FWD ? uc.y : -uc.y;
+      } else {
+        const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
+        auto uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp * ls_bytes)));
+        ur = (T)uc.x;
+        ui = FWD ? (T)uc.y : -(T)uc.y;
+      }
 #pragma unroll
       for (int u = 0; u < 2; u++)
 #pragma unroll
@@ -443,7 +472,7 @@ struct HopAcc<T, N, R, true> {
   }
 };
 
-template <int P, int N, int R, bool PK, int MU, bool FWD>
+template <int P, int N, int R, bool PK, int MU, bool FWD, bool RC>
 __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK>& acc, const DslashArgs& A,
                                        const typename Store<P>::elem* __restrict__ in,
                                        const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
@@ -452,7 +481,7 @@ __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK
   if constexpr (PK)
     hop_pk<P, N, R, MU, FWD>(acc.re, acc.im, A, in, gauge, link_off, nb, rhs0, bc, f);
   else
-    hop<P, N, R, MU, FWD>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
+    hop<P, N, R, MU, FWD, RC>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
 }
 
 }  // namespace detail
@@ -571,13 +600,15 @@ struct RegCap {
 };
 
 // PK: FP32 arithmetic on the packed FP32x2 pipe (FP32 / 16-bit storage only).
-template <int P, int N, int R, int MINB, bool PK>
+// RC: SU(3) links read as their first two rows (gauge12), the third reconstructed.
+template <int P, int N, int R, int MINB, bool PK, bool RC = false>
 __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashArgs A) {
   using S = Store<P>;
   using T = typename S::real;
   using E = typename S::elem;
   using namespace detail;
   static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
+  static_assert(!(PK && RC), "no packed variant with link reconstruction");
 
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, grp;
@@ -603,8 +634,8 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
   const uint32_t vh = A.geo.vh;
   const uint32_t nrhs = A.nrhs;
   const E* __restrict__ in = static_cast<const E*>(A.in);
-  const E* __restrict__ gauge = static_cast<const E*>(A.gauge);
-  constexpr uint32_t NN = N * N;
+  const E* __restrict__ gauge = static_cast<const E*>(RC ? A.gauge12 : A.gauge);
+  constexpr uint32_t NN = RC ? (N - 1) * N : N * N;  // stored components per link
 
   HopAcc<T, N, R, PK> hacc;
   hacc.zero();
@@ -616,21 +647,21 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
   {  // X
     const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
     const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-    hop_any<P, N, R, PK, 0, true>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 0, false>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Y
     const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
     const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
-    hop_any<P, N, R, PK, 1, true>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 1, false>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // Z
     const uint32_t pl = A.geo.plane;
     const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
     const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
-    hop_any<P, N, R, PK, 2, true>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 2, false>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
   }
   {  // T, with the optional antiperiodic sign
     const uint32_t cb = A.geo.cube;
@@ -639,8 +670,8 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
     const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
     const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
     const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
-    hop_any<P, N, R, PK, 3, true>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
-    hop_any<P, N, R, PK, 3, false>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
+    hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
+    hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
   }
 
   C2<T> acc[4][N][R];
@@ -650,12 +681,12 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
 }
 
 // host-side launcher of one instantiation
-template <int P, int N, int R, int MINB, bool PK = false>
+template <int P, int N, int R, int MINB, bool PK = false, bool RC = false>
 void launch_wilson_mrhs(const DslashArgs& A, int block, cudaStream_t stream) {
   const int groups = A.nrhs / R;
   const int64_t threads = (int64_t)A.geo.vh * groups;
   const int grid = (int)((threads + block - 1) / block);
-  wilson_mrhs_kernel<P, N, R, MINB, PK><<<grid, block, 0, stream>>>(A);
+  wilson_mrhs_kernel<P, N, R, MINB, PK, RC><<<grid, block, 0, stream>>>(A);
 }
 
 }  // namespace qcu

@@ -17,6 +17,8 @@
 // lexicographic: the lexicographic -> even-odd map is applied on the fly.
 #include <algorithm>
 
+#include <cstring>
+
 #include "layout.h"
 
 namespace qcu {
@@ -193,6 +195,53 @@ __global__ void convert_gauge_kernel(const double2* __restrict__ src, void* dst,
   }
 }
 
+// SU(3) links stored as their first two rows ([8][6][Vh] from the FP64 master
+// [8][9][Vh]: components 0..5 of every (mu, parity) block), converted to P
+template <int P>
+__global__ void compress_gauge_kernel(const double2* __restrict__ src, void* dst, int64_t vh) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  const int64_t count = 8 * 6 * vh;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    const int64_t blk = i / (6 * vh), rem = i - blk * 6 * vh;  // rem = comp * vh + site, comp < 6
+    const double2 v = src[blk * 9 * vh + rem];
+    E e;
+    if constexpr (P == PREC_DOUBLE) {
+      e = v;
+    } else if constexpr (P == PREC_SINGLE) {
+      e = make_float2((float)v.x, (float)v.y);
+    } else {
+      e = S::from_c(make_float2((float)v.x, (float)v.y));
+    }
+    static_cast<E*>(dst)[i] = e;
+  }
+}
+
+// max over links of |row 2 - conj(row 0 x row 1)| (FP64 master [8][9][Vh]);
+// the maximum of non-negative floats as their bit patterns
+__global__ void su3_row_check_kernel(const double2* __restrict__ g, int64_t vh, unsigned* out) {
+  const int64_t n = 8 * vh;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float mx = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t blk = i / vh, site = i - blk * vh;
+    double2 u[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) u[k] = g[(blk * 9 + k) * vh + site];
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int k = (j + 1) % 3, l = (j + 2) % 3;
+      // conj(u0k u1l - u0l u1k)
+      const double re = (u[k].x * u[3 + l].x - u[k].y * u[3 + l].y) - (u[l].x * u[3 + k].x - u[l].y * u[3 + k].y);
+      const double im = (u[k].x * u[3 + l].y + u[k].y * u[3 + l].x) - (u[l].x * u[3 + k].y + u[l].y * u[3 + k].x);
+      const double dr = u[6 + j].x - re, di = u[6 + j].y + im;
+      mx = fmaxf(mx, (float)sqrt(dr * dr + di * di));
+    }
+  }
+  atomicMax(out, __float_as_uint(mx));
+}
+
 // [rows][cols] -> [cols][rows] complex double transpose through shared memory
 __global__ void transpose_c64_kernel(const double2* __restrict__ src, double2* __restrict__ dst, int rows, int cols) {
   __shared__ double2 tile[32][33];
@@ -339,6 +388,34 @@ void convert_gauge(const void* src_fp64, int prec, void* dst, int64_t count, cud
     default: throw Error(QCU_ERR_UNSUPPORTED, "bad precision");
   }
   QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, cudaStream_t st) {
+  const int block = 256;
+  const int grid = (int)std::min<int64_t>((48 * vh + block - 1) / block, 152 * 32);
+  const double2* s = static_cast<const double2*>(src_fp64);
+  switch (prec) {
+    case PREC_DOUBLE: compress_gauge_kernel<PREC_DOUBLE><<<grid, block, 0, st>>>(s, dst, vh); break;
+    case PREC_SINGLE: compress_gauge_kernel<PREC_SINGLE><<<grid, block, 0, st>>>(s, dst, vh); break;
+    case PREC_HALF: compress_gauge_kernel<PREC_HALF><<<grid, block, 0, st>>>(s, dst, vh); break;
+    case PREC_BF16: compress_gauge_kernel<PREC_BF16><<<grid, block, 0, st>>>(s, dst, vh); break;
+    default: throw Error(QCU_ERR_UNSUPPORTED, "bad precision");
+  }
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st) {
+  QCU_CHECK_CUDA(cudaMemsetAsync(scratch, 0, sizeof(unsigned), st));
+  const int block = 256;
+  const int grid = (int)std::min<int64_t>((8 * vh + block - 1) / block, 152 * 8);
+  su3_row_check_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), vh, scratch);
+  QCU_CHECK_CUDA(cudaGetLastError());
+  unsigned v = 0;
+  QCU_CHECK_CUDA(cudaMemcpyAsync(&v, scratch, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st));
+  float f;
+  memcpy(&f, &v, sizeof(f));
+  return (double)f;
 }
 
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st) {

@@ -36,6 +36,13 @@ void convert_field(int prec_in, const void* src, const float* src_norm, int prec
                    int64_t vh, int ncomp, int nrhs, cudaStream_t st, const int* mask = nullptr);
 // FP64 internal gauge -> the same layout in `prec` (no scales: |U_ab| <= 1)
 void convert_gauge(const void* src_fp64, int prec, void* dst, int64_t count, cudaStream_t st);
+// SU(3) gauge compression (the reference's loadGauge2 keeps the first N - 1
+// rows, include/kernels/storageLoadStore/loadAndStore.cuh:17-27): the first
+// two rows of every link, [8][6][Vh] in precision prec
+void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, cudaStream_t st);
+// max over the links of |row 2 - conj(row 0 x row 1)| (0 for exact SU(3));
+// scratch: one device unsigned
+double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st);
 // plain complex-double transpose [rows][cols] -> [cols][rows]
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st);
 

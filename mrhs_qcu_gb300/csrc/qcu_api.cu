@@ -407,29 +407,30 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     QCU_REQUIRE(count != nullptr && (shapes != nullptr || max_shapes == 0) && max_shapes >= 0,
                 QCU_ERR_INVALID_ARGUMENT, "qcuDslashKernels: bad output arrays");
     int n = 0;
-    auto put = [&](int R, int m, int pk, int st) {
+    auto put = [&](int R, int m, int pk, int st, int rc) {
       if (n < max_shapes) {
-        shapes[4 * n] = R;
-        shapes[4 * n + 1] = m;
-        shapes[4 * n + 2] = pk;
-        shapes[4 * n + 3] = st;
+        shapes[5 * n] = R;
+        shapes[5 * n + 1] = m;
+        shapes[5 * n + 2] = pk;
+        shapes[5 * n + 3] = st;
+        shapes[5 * n + 4] = rc;
       }
       n++;
     };
     for (int R = 1; R <= 8; R++)
-      for (int pk = 0; pk < 2; pk++)
+      for (int v = 0; v < 3; v++)
         for (int m = 1; m <= 7; m++)
-          if (qcu::find_dslash(precision, nColors, R, m, pk)) put(R, m, pk, 0);
+          if (qcu::find_dslash(precision, nColors, R, m, v == 1, v == 2)) put(R, m, v == 1, 0, v == 2);
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
-    for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i]);
-    if (qcu::find_tc(precision, nColors)) put(1, 0, 0, -1);
+    for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0);
+    if (qcu::find_tc(precision, nColors)) put(1, 0, 0, -1, 0);
     *count = n;
   });
 }
 
 int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed,
-                  int* stages) {
+                  int* stages, int* recon) {
   return guarded([&] {
     Session& s = session();
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -439,6 +440,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (fi.norm) QCU_CHECK_CUDA(cudaMemsetAsync(fi.norm, 0, s.norm_bytes(precision, nrhs), s.stream()));
     qcu::DslashArgs A;
     A.gauge = s.gauge(precision);
+    A.gauge12 = s.gauge12(precision);
     A.in = fi.data;
     A.in_norm = fi.norm;
     A.out = fo.data;
@@ -461,6 +463,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (min_blocks) *min_blocks = c.minb;
     if (packed) *packed = c.pk;
     if (stages) *stages = c.tc ? -1 : c.tma;
+    if (recon) *recon = c.rc;
   });
 }
 

@@ -64,6 +64,7 @@ void Autotuner::load_file() {
     if (!(ls >> k >> c.R >> c.block >> c.minb >> c.pk)) continue;
     if (!(ls >> c.tma >> c.rcta)) c.tma = c.rcta = 0;
     if (!(ls >> c.tc)) c.tc = 0;
+    if (!(ls >> c.rc)) c.rc = 0;
     cache_[k] = c;
   }
 }
@@ -74,26 +75,29 @@ void Autotuner::save_file() {
   std::ofstream out(path);
   for (auto& kv : cache_)
     out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << " " << kv.second.pk
-        << " " << kv.second.tma << " " << kv.second.rcta << " " << kv.second.tc << "\n";
+        << " " << kv.second.tma << " " << kv.second.rcta << " " << kv.second.tc << " " << kv.second.rc << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
-  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta[,tensor]]]]]" pins the kernel shape
-  // (profiling, sweeps); stages > 0 selects the TMA-staged kernel, tensor = 1 the tensor-core kernel
-  // (the other fields are then ignored)
+  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta[,tensor[,recon]]]]]]" pins the kernel
+  // shape (profiling, sweeps); stages > 0 selects the TMA-staged kernel, tensor = 1 the tensor-core
+  // kernel (the other fields are then ignored); recon = 1 the register kernel on two-row SU(3) links
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc);
+    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc,
+                           &c.rc);
+    if (got < 8) c.rc = 0;
     const bool tensor = got >= 7 && c.tc == 1 && find_tc(prec, N);
     const bool staged = !tensor && got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 &&
                         find_tma(prec, N, c.R, c.tma);
     const bool plain = !tensor && got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
-                       find_dslash(prec, N, c.R, c.minb, c.pk) && c.block >= 32 && c.block <= 256 &&
+                       find_dslash(prec, N, c.R, c.minb, c.pk, c.rc) && c.block >= 32 && c.block <= 256 &&
                        c.block % 32 == 0;
     if (tensor || staged || plain) {
       if (!staged) c.tma = c.rcta = 0;
       if (!tensor) c.tc = 0;
+      if (!plain) c.rc = 0;
       *found = true;
       return c;
     }
@@ -142,9 +146,11 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   float best_ms = 1e30f;
   for (int i = 0; i < n; i++) {
     if (A.nrhs % opts[i]) continue;
-    for (int pk = 0; pk < 2; pk++) {
+    for (int v = 0; v < 3; v++) {  // plain, packed FP32x2, two-row links
+    const int pk = v == 1, rc = v == 2;
+    if (rc && !A.gauge12) continue;
     int minbs[8];
-    const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8);
+    const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8, rc);
     for (int j = 0; j < nm; j++)
       for (int b : blocks) {
         DslashConfig c;
@@ -152,6 +158,7 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
         c.block = b;
         c.minb = minbs[j];
         c.pk = pk;
+        c.rc = rc;
         launch_dslash(A, prec, N, c, st);  // warm-up
         QCU_CHECK_CUDA(cudaEventRecord(e0, st));
         const int reps = 3;
@@ -257,8 +264,9 @@ void Session::load_gauge(const void* caller_gauge, int lex) {
   const size_t bytes = (size_t)8 * geo.vh * N * N * 16;
   void* d = gauge_[PREC_DOUBLE].ensure(bytes);
   pack_gauge(PREC_DOUBLE, N, caller_gauge, lex, d, geo, stream());
-  for (int p = 0; p < 5; p++) gauge_valid_[p] = false;
+  for (int p = 0; p < 5; p++) gauge_valid_[p] = gauge12_valid_[p] = false;
   gauge_valid_[PREC_DOUBLE] = true;
+  su3_dev_ = -1.0;
   gauge_loaded_ = true;
 }
 
@@ -273,6 +281,25 @@ const void* Session::gauge(int prec) {
     gauge_valid_[prec] = true;
   }
   return gauge_[prec].get();
+}
+
+const void* Session::gauge12(int prec) {
+  QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
+  QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  if (N != 3) return nullptr;
+  if (su3_dev_ < 0) {
+    unsigned* scratch = static_cast<unsigned*>(su3_scratch_.ensure(16));
+    su3_dev_ = su3_row_deviation(gauge_[PREC_DOUBLE].get(), geo.vh, scratch, stream());
+  }
+  // a reconstructed row must agree with the stored one to the rounding of the precision
+  const double tol = prec == PREC_DOUBLE ? 1e-13 : (prec == PREC_SINGLE ? 1e-7 : 1e-4);
+  if (!(su3_dev_ < tol)) return nullptr;
+  if (!gauge12_valid_[prec]) {
+    void* d = gauge12_[prec].ensure((size_t)48 * geo.vh * prec_complex_bytes(prec));
+    compress_gauge_su3(gauge_[PREC_DOUBLE].get(), prec, d, geo.vh, stream());
+    gauge12_valid_[prec] = true;
+  }
+  return gauge12_[prec].get();
 }
 
 FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {
@@ -294,6 +321,7 @@ void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagg
               "dslash operands must share nrhs");
   DslashArgs A;
   A.gauge = gauge(in.prec);
+  A.gauge12 = gauge12(in.prec);
   A.in = in.data;
   A.in_norm = in.norm;
   A.out = out.data;

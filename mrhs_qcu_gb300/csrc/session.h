@@ -147,6 +147,10 @@ class Session {
   void load_gauge(const void* caller_gauge, int lex);
   bool gauge_loaded() const { return gauge_loaded_; }
   const void* gauge(int prec);  // internal gauge in `prec`, converted once
+  // SU(3) only: the gauge as the first two rows of every link ([8][6][Vh] in
+  // `prec`), or nullptr when the loaded field is not SU(3) to that precision's
+  // rounding (then the third rows are not reconstructible)
+  const void* gauge12(int prec);
 
   // ---- fields ------------------------------------------------------------
   size_t field_elems(int nrhs) const { return (size_t)geo.vh * 4 * N * nrhs; }
@@ -169,6 +173,10 @@ class Session {
   bool gauge_loaded_ = false;
   DeviceBuffer gauge_[5];
   bool gauge_valid_[5] = {false, false, false, false, false};
+  DeviceBuffer gauge12_[5];
+  bool gauge12_valid_[5] = {false, false, false, false, false};
+  double su3_dev_ = -1.0;  // max |row 2 - conj(row 0 x row 1)|, < 0: not measured
+  DeviceBuffer su3_scratch_;
   std::unique_ptr<Blas> blas_;
   DeviceBuffer partials_;
   DeviceBuffer scalars_;

@@ -72,22 +72,42 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     assert shapes
     outs = {}
     try:
-        for i, (R, minb, pk, st) in enumerate(shapes):
+        for i, (R, minb, pk, st, rc) in enumerate(shapes):
             if nrhs % R:
                 continue
-            os.environ["QCU_DSLASH_CONFIG"] = ("1,0,0,0,0,0,1" if st < 0 else
-                                               "%d,%d,%d,%d,%d" % (R, (32, 64, 128, 256)[i % 4], minb, pk, st))
+            os.environ["QCU_DSLASH_CONFIG"] = ("1,0,0,0,0,0,1" if st < 0 else "%d,%d,%d,%d,%d,0,0,%d" % (
+                R, (32, 64, 128, 256)[i % 4], minb, pk, st, rc))
             for d in (0, 1):  # (parity 0, dagger 0) and (parity 1, dagger 1)
                 got = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
-                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, d)
-                outs[(R, minb, pk, st, d)] = got
+                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, rc, d)
+                outs[(R, minb, pk, st, rc, d)] = got
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
-    for (R, minb, pk, st, d), got in outs.items():
+    for (R, minb, pk, st, rc, d), got in outs.items():
         if pk or st > 0:
-            for (r2, m2, p2, s2, d2), other in outs.items():
-                if r2 == R and d2 == d and not p2 and not s2:
+            for (r2, m2, p2, s2, rc2, d2), other in outs.items():
+                if r2 == R and d2 == d and not p2 and not s2 and not rc2:
                     assert np.array_equal(got, other), (R, minb, pk, st, m2, d)
+
+
+@pytest.mark.parametrize("prec", [2, 1, 4])
+def test_reconstructed_links_only_for_su3_fields(cuda, qcu_lib, prec):
+    """The two-row (reconstruct-12) kernels: exact against the oracle on an
+    SU(3) field; on a field that is not SU(3) (links scaled by 1.01) the
+    library keeps the full links, so the result is still the oracle's."""
+    Q = qcu_lib
+    L, nrhs = (4, 4, 4, 8), 4
+    g = S.random_gauge(L, 3, seed=97)
+    psi = S.random_fermions(L, 3, nrhs, seed=98)
+    R = 1 if prec == 2 else 2
+    minb = 1 if prec != 4 else 2
+    os.environ["QCU_DSLASH_CONFIG"] = "%d,64,%d,0,0,0,0,1" % (R, minb)
+    try:
+        for gauge in (g, 1.01 * g):
+            got = abi_dslash(cuda, Q, psi, gauge, L, 1, 0, prec, antiperiodic_t=True)
+            assert rel(got, O.dslash(psi, gauge, L, 1, 0, True)) < TOL[prec]
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
 
 
 @pytest.mark.parametrize("n,nrhs", [(4, 16), (8, 16), (6, 24), (8, 64), (5, 128)])
