@@ -97,6 +97,21 @@ int qcuDslashMRHS(void *out, void *out_norm, const void *in, const void *in_norm
 int qcuDslashXpayMRHS(void *out, void *out_norm, const void *in, const void *in_norm, const void *x,
                       const void *x_norm, int nrhs, int parity, int dagger, int precision, double a, double b);
 
+/* Clover term A of the Wilson-clover operator M = A - kappa D.  The
+ * reference reserves DSLASH_CLOVER (include/qcu_enum.h:12) and the per-site
+ * storage of (Nc*Ns)^2/2 complex (include/basic_data/qcu_point.cuh:98-101)
+ * but has no clover code; this layout follows that storage:
+ *   clover [parity=2][Vh][block=2][2N][2N] complex double (device), block 0
+ *   acting on spins 0, 1 and block 1 on spins 2, 3, row / column index =
+ *   local spin * N + colour; the blocks must be Hermitian.
+ * qcuLoadClover copies it and inverts every block once (FP64); a singular
+ * block returns QCU_ERR_INVALID_ARGUMENT.  The solvers use it when
+ * QcuSolverParam.use_clover = 1. */
+int qcuLoadClover(void *clover);
+/* out = A_parity in (inverse = 1: A_parity^-1 in) on resident MRHS fields */
+int qcuCloverMRHS(void *out, void *out_norm, const void *in, const void *in_norm, int nrhs, int parity, int inverse,
+                  int precision);
+
 /* out[r] = |field_r|^2 (FP64 accumulation, deterministic order) for each RHS
  * of a resident MRHS field of the session lattice, precision FP32 or FP64.
  * out is a device array of nrhs doubles.  The block partial sums live in the
@@ -157,6 +172,7 @@ typedef struct QcuSolverParam_s {
   double delta;        /* reliable-update trigger: |r| < delta * max|r| since the last update */
   int use_graph;       /* capture inner iterations in CUDA graphs */
   int src_mode;        /* QCU_SRC_EO_FULL or QCU_SRC_LEX for x and b */
+  int use_clover;      /* 1: M = A - kappa D with the clover field of qcuLoadClover */
   /* outputs */
   int iterations;
   int reliable_updates;

@@ -62,7 +62,8 @@ class QcuGrid(ctypes.Structure):
 class QcuSolverParam(ctypes.Structure):
     _fields_ = [("solver", ctypes.c_int), ("inner_precision", ctypes.c_int), ("kappa", ctypes.c_double),
                 ("tol", ctypes.c_double), ("max_iter", ctypes.c_int), ("delta", ctypes.c_double),
-                ("use_graph", ctypes.c_int), ("src_mode", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("use_graph", ctypes.c_int), ("src_mode", ctypes.c_int), ("use_clover", ctypes.c_int),
+                ("iterations", ctypes.c_int),
                 ("reliable_updates", ctypes.c_int), ("seconds", ctypes.c_double),
                 ("true_residual", ctypes.c_double * 256), ("converged", ctypes.c_int * 256)]
 
@@ -74,7 +75,7 @@ EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcu
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
                "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
-               "qcuNorm2MRHSNoAlloc",
+               "qcuNorm2MRHSNoAlloc", "qcuLoadClover", "qcuCloverMRHS",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
 
@@ -135,6 +136,8 @@ def lib() -> ctypes.CDLL:
                            ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
         "qcuMeasureFmaRate": ([I, ctypes.POINTER(ctypes.c_double)], I),
+        "qcuLoadClover": ([P], I),
+        "qcuCloverMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuSolverParamDefaults": ([ctypes.POINTER(QcuSolverParam)], None),
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
         "qcuNorm2MRHS": ([P, P, I, I], I),
@@ -321,6 +324,16 @@ def dslash_kernels(precision: int, n_colors: int = 3):
     cnt = ctypes.c_int()
     _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
     return [tuple(arr[5 * i:5 * i + 5]) for i in range(min(cnt.value, 64))]
+
+
+def load_clover(clover_ptr) -> None:
+    """qcuLoadClover: clover field [2][Vh][2][2N][2N] complex double (device)."""
+    _raise_if(lib().qcuLoadClover(_p(clover_ptr)))
+
+
+def clover_mrhs(out, out_norm, inp, in_norm, nrhs: int, parity: int, inverse: int, precision: int) -> None:
+    _raise_if(lib().qcuCloverMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), int(nrhs), int(parity),
+                                  int(inverse), int(precision)))
 
 
 def measure_fma_rate(precision: int) -> float:

@@ -385,6 +385,36 @@ int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_
   });
 }
 
+int qcuLoadClover(void* clover) {
+  return guarded([&] {
+    Session& s = session();
+    s.load_clover(clover);
+    s.sync();
+  });
+}
+
+int qcuCloverMRHS(void* out, void* out_norm, const void* in, const void* in_norm, int nrhs, int parity, int inverse,
+                  int precision) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+    QCU_REQUIRE(nrhs >= 1, QCU_ERR_INVALID_ARGUMENT, "nrhs must be positive");
+    QCU_REQUIRE(out && in && out != in, QCU_ERR_INVALID_ARGUMENT, "null or in-place field");
+    QCU_REQUIRE(((uintptr_t)out | (uintptr_t)in) % 16 == 0, QCU_ERR_INVALID_ARGUMENT,
+                "fields must be 16-byte aligned");
+    QCU_REQUIRE(!qcu::prec_is16(precision) || (out_norm && in_norm), QCU_ERR_INVALID_ARGUMENT,
+                "16-bit fields need norm arrays");
+    qcu::FieldView fo, fi;
+    fo.data = out;
+    fo.norm = static_cast<float*>(out_norm);
+    fi.data = const_cast<void*>(in);
+    fi.norm = static_cast<float*>(const_cast<void*>(in_norm));
+    fo.prec = fi.prec = precision;
+    fo.nrhs = fi.nrhs = nrhs;
+    s.clover_apply(fo, fi, qcu::FieldView{}, parity, inverse != 0, 1.0, 0.0);
+  });
+}
+
 int qcuNorm2MRHS(double* out, const void* field, int precision, int nrhs) {
   return guarded([&] {
     Session& s = session();
@@ -561,6 +591,7 @@ int qcuInvert(void* const* x, void* const* b, int nrhs, QcuSolverParam* p) {
     q.delta = p->delta > 0 ? p->delta : 0.1;
     q.use_graph = p->use_graph != 0;
     q.src_mode = p->src_mode;
+    q.clover = p->use_clover != 0;
     qcu::SolveResult r = qcu::solve(s, x, b, nrhs, q);
     p->iterations = r.iterations;
     p->reliable_updates = r.reliable_updates;

@@ -6,6 +6,7 @@
 #include <sstream>
 
 #include "session.h"
+#include "clover.h"
 #include "dslash_tc.h"
 #include "dslash_tma.h"
 
@@ -300,6 +301,60 @@ const void* Session::gauge12(int prec) {
     gauge12_valid_[prec] = true;
   }
   return gauge12_[prec].get();
+}
+
+void Session::load_clover(const void* caller_clover) {
+  QCU_REQUIRE(caller_clover != nullptr, QCU_ERR_INVALID_ARGUMENT, "clover pointer is null");
+  const size_t bytes = (size_t)16 * geo.vh * N * N * 16;  // 2 parities x 2 blocks x (2N)^2 complex double
+  void* d = clover_[PREC_DOUBLE].ensure(bytes);
+  pack_clover(N, caller_clover, d, geo.vh, stream());
+  void* di = cloverinv_[PREC_DOUBLE].ensure(bytes);
+  int* flag = static_cast<int*>(clover_flag_.ensure(16));
+  const bool ok = invert_clover(N, d, di, geo.vh, flag, stream());
+  for (int p = 0; p < 5; p++) clover_valid_[p] = cloverinv_valid_[p] = false;
+  clover_valid_[PREC_DOUBLE] = cloverinv_valid_[PREC_DOUBLE] = true;
+  clover_loaded_ = ok;
+  QCU_REQUIRE(ok, QCU_ERR_INVALID_ARGUMENT, "clover field has a singular block");
+}
+
+const void* Session::clover(int prec, bool inverse) {
+  QCU_REQUIRE(clover_loaded_, QCU_ERR_NO_OPERATOR, "no clover field loaded");
+  QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  DeviceBuffer* buf = inverse ? cloverinv_ : clover_;
+  bool* valid = inverse ? cloverinv_valid_ : clover_valid_;
+  if (!valid[prec]) {
+    const int64_t count = (int64_t)16 * geo.vh * N * N;
+    void* d = buf[prec].ensure((size_t)count * prec_complex_bytes(prec));
+    convert_gauge(buf[PREC_DOUBLE].get(), prec, d, count, stream());
+    valid[prec] = true;
+  }
+  return buf[prec].get();
+}
+
+void Session::clover_apply(FieldView out, FieldView in, FieldView x, int parity, bool inverse, double a, double b,
+                           const int* mask, const float* a_rhs_f, const double* a_rhs_d) {
+  QCU_REQUIRE(parity == 0 || parity == 1, QCU_ERR_INVALID_ARGUMENT, "parity must be 0 or 1");
+  QCU_REQUIRE(out.prec == in.prec && (!x.data || x.prec == in.prec) && out.nrhs == in.nrhs,
+              QCU_ERR_INVALID_ARGUMENT, "clover operands must share precision and nrhs");
+  DslashArgs A;
+  A.gauge = nullptr;
+  A.in = in.data;
+  A.in_norm = in.norm;
+  A.out = out.data;
+  A.out_norm = out.norm;
+  A.x = x.data;
+  A.x_norm = x.norm;
+  A.mask = mask;
+  A.a_rhs_f = a_rhs_f;
+  A.a_rhs_d = a_rhs_d;
+  A.a = a;
+  A.b = b;
+  A.geo = geo;
+  A.nrhs = in.nrhs;
+  A.parity = parity;
+  A.dagger = 0;
+  A.antiperiodic_t = 0;
+  qcu::clover_apply(in.prec, N, A, clover(in.prec, inverse), stream());
 }
 
 FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {

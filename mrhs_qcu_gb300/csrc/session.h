@@ -152,6 +152,16 @@ class Session {
   // rounding (then the third rows are not reconstructible)
   const void* gauge12(int prec);
 
+  // ---- clover term (clover.h) ---------------------------------------------
+  // caller field [2][Vh][2][2N][2N] complex double, Hermitian blocks; packed
+  // to an FP64 master and inverted per site once
+  void load_clover(const void* caller_clover);
+  bool has_clover() const { return clover_loaded_; }
+  const void* clover(int prec, bool inverse);  // resident [2][2][(2N)^2][Vh] in `prec`
+  // out = a * C in + b * x, C = A_parity or A_parity^-1, on the library stream
+  void clover_apply(FieldView out, FieldView in, FieldView x, int parity, bool inverse, double a, double b,
+                    const int* mask = nullptr, const float* a_rhs_f = nullptr, const double* a_rhs_d = nullptr);
+
   // ---- fields ------------------------------------------------------------
   size_t field_elems(int nrhs) const { return (size_t)geo.vh * 4 * N * nrhs; }
   size_t field_bytes(int prec, int nrhs) const { return field_elems(nrhs) * prec_complex_bytes(prec); }
@@ -177,6 +187,10 @@ class Session {
   bool gauge12_valid_[5] = {false, false, false, false, false};
   double su3_dev_ = -1.0;  // max |row 2 - conj(row 0 x row 1)|, < 0: not measured
   DeviceBuffer su3_scratch_;
+  bool clover_loaded_ = false;
+  DeviceBuffer clover_[5], cloverinv_[5], clover_flag_;
+  bool clover_valid_[5] = {false, false, false, false, false};
+  bool cloverinv_valid_[5] = {false, false, false, false, false};
   std::unique_ptr<Blas> blas_;
   DeviceBuffer partials_;
   DeviceBuffer scalars_;
@@ -194,6 +208,7 @@ struct SolveRequest {
   double delta = 0.1;
   bool use_graph = true;
   int src_mode = SRC_EO_FULL;
+  bool clover = false;  // M = A - kappa D with the session's clover field A
 };
 struct SolveResult {
   int iterations = 0;

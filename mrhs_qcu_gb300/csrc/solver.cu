@@ -9,6 +9,10 @@
 // and Mhat^dag = 1 - kappa^2 D_eo^- D_oe^- (the dagger flag f = -1), because
 // D^dag = gamma5 D gamma5 is the hop with f = -1.  With x_o reconstructed
 // that way, |b - M x| over the full lattice equals |bhat - Mhat x_e|.
+// With a clover field (M = A - kappa D, A Hermitian and block diagonal in
+// chirality, so A commutes with gamma5):
+//   Mhat_r = A_ee - kappa_r^2 D_eo A_oo^-1 D_oe,  bhat_r = b_e + kappa_r D_eo A_oo^-1 b_o,
+//   x_o    = A_oo^-1 (b_o + kappa_r D_oe x_e),   Mhat^dag = Mhat with f = -1.
 //
 // CG  : CG on Mhat^dag Mhat that also tracks s = bhat - Mhat x (the residual
 //       of the actual system), so convergence is tested on |s| / |b|.
@@ -219,6 +223,8 @@ FieldRef SlotEngine::ref(const FieldView& f) const {
 size_t SlotEngine::bytes_needed(const Session& s, int capacity, int inner_prec) {
   const int kp = inner_prec == PREC_DOUBLE ? PREC_DOUBLE : PREC_SINGLE;
   size_t b = 8 * s.field_bytes(PREC_DOUBLE, capacity) + 7 * s.field_bytes(kp, capacity);
+  if (s.has_clover()) b += s.field_bytes(PREC_DOUBLE, capacity) + s.field_bytes(inner_prec, capacity) +
+                           s.norm_bytes(inner_prec, capacity);
   if (inner_prec != kp) b += 3 * (s.field_bytes(inner_prec, capacity) + s.norm_bytes(inner_prec, capacity));
   b += s.field_bytes(inner_prec, capacity) + s.norm_bytes(inner_prec, capacity);
   return b;
@@ -255,6 +261,12 @@ SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const st
     wop_ = s.alloc_field(t + "wop", op_, n_);
   }
   tmpop_ = s.alloc_field(t + "tmpop", op_, n_);
+  cl_ = q.clover;
+  QCU_REQUIRE(!cl_ || s.has_clover(), QCU_ERR_NO_OPERATOR, "clover solve requested but no clover field loaded");
+  if (cl_) {
+    tmp64b_ = s.alloc_field(t + "tmp64b", PREC_DOUBLE, n_);
+    tmpopb_ = s.alloc_field(t + "tmpopb", op_, n_);
+  }
   // per-slot device scalars
   const int R = QCU_MAX_RHS;
   char* d = static_cast<char*>(s.ws.get(t + "scalars", (size_t)R * 64 * sizeof(double) + 4096));
@@ -296,7 +308,7 @@ SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const st
   QCU_CHECK_CUDA(cudaMemsetAsync(d, 0, (size_t)R * 64 * sizeof(double) + 4096, st_));
   // every field starts at zero: masked slots never meet uninitialised memory
   for (FieldView* f : {&be_, &bo_, &bh_, &xh_, &xo_, &sh_, &th_, &tmp64_, &xl_, &sl_, &rl_, &pl_, &ql_, &wl_, &r0l_,
-                       &pop_, &qop_, &wop_, &tmpop_}) {
+                       &pop_, &qop_, &wop_, &tmpop_, &tmp64b_, &tmpopb_}) {
     if (!f->data) continue;
     QCU_CHECK_CUDA(cudaMemsetAsync(f->data, 0, s.field_bytes(f->prec, n_), st_));
     if (f->norm) QCU_CHECK_CUDA(cudaMemsetAsync(f->norm, 0, s.norm_bytes(f->prec, n_), st_));
@@ -348,22 +360,29 @@ void SlotEngine::upload_kappa() {
 
 // out = Mhat in (dagger 0) or Mhat^dag in (dagger 1) for the slots in mask,
 // fields in precision `prec` with per-slot kappa
-void SlotEngine::apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, int dagger,
-                            const int* mask) {
+void SlotEngine::apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, const FieldView& tmp2,
+                            int dagger, const int* mask) {
   s_.hop(tmp, in, FieldView{}, 1, dagger, 1.0, 0.0, mask);
+  FieldView hop_in = tmp, x = in;
+  if (cl_) {  // A_oo^-1 D_oe in, and A_ee in for the xpay term
+    s_.clover_apply(tmp2, tmp, FieldView{}, 1, true, 1.0, 0.0, mask);
+    s_.clover_apply(tmp, in, FieldView{}, 0, false, 1.0, 0.0, mask);
+    hop_in = tmp2;
+    x = tmp;
+  }
   if (in.prec == PREC_DOUBLE)
-    s_.hop(out, tmp, in, 0, dagger, 0.0, 1.0, mask, nullptr, S_.nk2_d);
+    s_.hop(out, hop_in, x, 0, dagger, 0.0, 1.0, mask, nullptr, S_.nk2_d);
   else
-    s_.hop(out, tmp, in, 0, dagger, 0.0, 1.0, mask, S_.nk2_f, nullptr);
+    s_.hop(out, hop_in, x, 0, dagger, 0.0, 1.0, mask, S_.nk2_f, nullptr);
 }
 
 // Krylov-precision out = Mhat in (or Mhat^dag) for the slots in mask
 void SlotEngine::op_apply(const FieldView& out_kp, const FieldView& in_kp, int dagger, const int* mask) {
   if (op_ == kp_) {
-    apply_mhat(out_kp, in_kp, tmpop_, dagger, mask);
+    apply_mhat(out_kp, in_kp, tmpop_, tmpopb_, dagger, mask);
   } else {
     convert_field(kp_, in_kp.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_, mask);
-    apply_mhat(qop_, pop_, tmpop_, dagger, mask);
+    apply_mhat(qop_, pop_, tmpop_, tmpopb_, dagger, mask);
     convert_field(op_, qop_.data, qop_.norm, kp_, out_kp.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, mask);
   }
 }
@@ -371,12 +390,12 @@ void SlotEngine::op_apply(const FieldView& out_kp, const FieldView& in_kp, int d
 void SlotEngine::cg_iteration() {
   Blas& B = s_.blas();
   if (op_ == kp_) {
-    apply_mhat(ql_, pl_, tmpop_, 0, S_.active);
-    apply_mhat(wl_, ql_, tmpop_, 1, S_.active);
+    apply_mhat(ql_, pl_, tmpop_, tmpopb_, 0, S_.active);
+    apply_mhat(wl_, ql_, tmpop_, tmpopb_, 1, S_.active);
   } else {
     convert_field(kp_, pl_.data, nullptr, op_, pop_.data, pop_.norm, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
-    apply_mhat(qop_, pop_, tmpop_, 0, S_.active);
-    apply_mhat(wop_, qop_, tmpop_, 1, S_.active);
+    apply_mhat(qop_, pop_, tmpop_, tmpopb_, 0, S_.active);
+    apply_mhat(wop_, qop_, tmpop_, tmpopb_, 1, S_.active);
     convert_field(op_, qop_.data, qop_.norm, kp_, ql_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
     convert_field(op_, wop_.data, wop_.norm, kp_, wl_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
   }
@@ -451,7 +470,7 @@ void SlotEngine::restart(const std::vector<int>& slots, bool fresh) {
     B.axpby(S_.zero, ref(pl_), S_.ck, ref(pl_), st_);  // p = 0
   }
   // s = bhat - Mhat x  (only the selected slots are computed)
-  apply_mhat(th_, xh_, tmp64_, 0, S_.sel);
+  apply_mhat(th_, xh_, tmp64_, tmp64b_, 0, S_.sel);
   B.axpby(S_.cm, ref(bh_), S_.ck, ref(sh_), st_);
   B.axpby_norm(S_.cn, ref(th_), nullptr, ref(sh_), S_.ss_true, st_);
   std::vector<double> ss(n_);
@@ -540,9 +559,14 @@ void SlotEngine::admit(const std::vector<int>& slots, void* const* b, const doub
     stop2[r] = h.stop2;
   }
   QCU_CHECK_CUDA(cudaMemcpyAsync(S_.stop2, stop2.data(), sizeof(double) * n_, cudaMemcpyHostToDevice, st_));
-  // bhat = b_e + kappa_r D_eo b_o for the new slots
+  // bhat = b_e + kappa_r D_eo b_o (clover: b_e + kappa_r D_eo A_oo^-1 b_o) for the new slots
   upload_sel(slots);
-  s_.hop(bh_, bo_, be_, 0, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  if (cl_) {
+    s_.clover_apply(tmp64b_, bo_, FieldView{}, 1, true, 1.0, 0.0, S_.sel);
+    s_.hop(bh_, tmp64b_, be_, 0, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  } else {
+    s_.hop(bh_, bo_, be_, 0, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  }
   restart(slots, true);
 }
 
@@ -585,8 +609,13 @@ void SlotEngine::retire(const std::vector<int>& slots, void* const* x, int src_m
     px.p[r] = x[i];
   }
   upload_sel(slots);
-  // x_o = b_o + kappa_r D_oe x_e
-  s_.hop(xo_, xh_, bo_, 1, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  // x_o = b_o + kappa_r D_oe x_e (clover: A_oo^-1 of it)
+  if (cl_) {
+    s_.hop(tmp64b_, xh_, bo_, 1, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+    s_.clover_apply(xo_, tmp64b_, FieldView{}, 1, true, 1.0, 0.0, S_.sel);
+  } else {
+    s_.hop(xo_, xh_, bo_, 1, 0, 0.0, 1.0, S_.sel, nullptr, S_.kap_d);
+  }
   unpack_fermions(PREC_DOUBLE, s_.N, px, src_mode, 0, xh_.data, nullptr, s_.geo, n_, st_);
   unpack_fermions(PREC_DOUBLE, s_.N, px, src_mode, 1, xo_.data, nullptr, s_.geo, n_, st_);
   QCU_CHECK_CUDA(cudaStreamSynchronize(st_));

@@ -60,7 +60,8 @@ class SlotEngine {
   FieldRef ref(const FieldView& f) const;
   void upload_sel(const std::vector<int>& slots);
   void upload_kappa();
-  void apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, int dagger, const int* mask);
+  void apply_mhat(const FieldView& out, const FieldView& in, const FieldView& tmp, const FieldView& tmp2, int dagger,
+                  const int* mask);
   void op_apply(const FieldView& out_kp, const FieldView& in_kp, int dagger, const int* mask);
   void cg_iteration();
   void bicg_iteration();
@@ -76,6 +77,8 @@ class SlotEngine {
   FieldView be_, bo_, bh_, xh_, xo_, sh_, th_, tmp64_;
   FieldView xl_, sl_, rl_, pl_, ql_, wl_, r0l_;
   FieldView pop_, qop_, wop_, tmpop_;
+  FieldView tmp64b_, tmpopb_;  // second temporaries of the clover operator
+  bool cl_ = false;            // Wilson-clover: M = A - kappa D
   SolverScalars S_{};
   std::vector<SlotState> host_;
   cudaGraphExec_t graph_exec_ = nullptr;

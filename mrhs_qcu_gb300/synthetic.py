@@ -121,3 +121,15 @@ def random_sun_torch(count: int, n: int, generator, device="cuda", chunk: int = 
                 a[:, k + 1:, :] -= f.unsqueeze(2) * a[:, k:k + 1, :]
         out[s:s + m] = q * (det ** (-1.0 / n)).view(-1, 1, 1)
     return out
+
+
+def random_clover(L, n: int, eps: float = 0.1, seed: int = 3) -> np.ndarray:
+    """A clover-like field: per site two Hermitian (2n x 2n) blocks
+    1 + eps * H, H Hermitian with Gaussian entries, in the caller layout
+    (2, Vh, 2, 2n, 2n) complex double (positive definite for small eps)."""
+    vh = half_volume(L)
+    rng = np.random.default_rng(seed)
+    m = 2 * n
+    h = rng.standard_normal((2, vh, 2, m, m)) + 1j * rng.standard_normal((2, vh, 2, m, m))
+    h = 0.5 * (h + np.conj(np.swapaxes(h, -1, -2)))
+    return np.eye(m, dtype=np.complex128) + eps * h

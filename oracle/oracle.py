@@ -47,10 +47,11 @@ def lib():
         _lib.oracle_dslash.argtypes = [P, P, P, P, I, I, I, I, I]
         _lib.oracle_lex_to_eo.argtypes = [P, P, P, I]
         _lib.oracle_eo_to_lex.argtypes = [P, P, P, I]
-        _lib.oracle_wilson_full.argtypes = [P, P, P, P, I, D, I, I, P]
-        _lib.oracle_cgnr_full.argtypes = [P, P, P, P, I, D, I, D, I, ctypes.POINTER(D)]
+        _lib.oracle_clover_apply.argtypes = [P, P, P, P, I, I, I, I]
+        _lib.oracle_wilson_full.argtypes = [P, P, P, P, P, I, D, I, I, P]
+        _lib.oracle_cgnr_full.argtypes = [P, P, P, P, P, I, D, I, D, I, ctypes.POINTER(D)]
         _lib.oracle_cgnr_full.restype = I
-        _lib.oracle_true_residual.argtypes = [P, P, P, P, I, D, I]
+        _lib.oracle_true_residual.argtypes = [P, P, P, P, P, I, D, I]
         _lib.oracle_true_residual.restype = D
         _lib.oracle_num_threads.restype = I
         _lib.oracle_set_num_threads.argtypes = [I]
@@ -108,38 +109,60 @@ def eo_to_lex(eo: np.ndarray, L) -> np.ndarray:
     return lex
 
 
+def _clover_ptr(clover):
+    """(pointer, array kept alive by the caller) of an optional clover field."""
+    if clover is None:
+        return None, None
+    c = _c128(clover)
+    return _ptr(c), c
+
+
+def clover_apply(psi: np.ndarray, clover: np.ndarray, L, parity: int, dagger: int = 0) -> np.ndarray:
+    """A_parity psi for psi (nrhs, Vh, 4, N); clover (2, Vh, 2, 2N, 2N)."""
+    psi = _c128(psi)
+    clover = _c128(clover)
+    out = np.empty_like(psi)
+    lib().oracle_clover_apply(_ptr(out), _ptr(psi), _ptr(clover), _dims(L), psi.shape[-1], psi.shape[0],
+                              int(parity), int(dagger))
+    return out
+
+
 def wilson_full(x: np.ndarray, gauge: np.ndarray, L, kappa: float, dagger: int = 0,
-                antiperiodic_t: bool = False) -> np.ndarray:
-    """M x = x - kappa D x on a full eo field (2, Vh, 4, N)."""
+                antiperiodic_t: bool = False, clover=None) -> np.ndarray:
+    """M x = A x - kappa D x on a full eo field (2, Vh, 4, N); A = 1 without
+    a clover field (2, Vh, 2, 2N, 2N)."""
     x = _c128(x)
     gauge = _c128(gauge)
+    cp, keep = _clover_ptr(clover)
     n = x.shape[-1]
     out = np.empty_like(x)
-    sc = np.empty(x.shape[1:], dtype=np.complex128)
-    lib().oracle_wilson_full(_ptr(out), _ptr(x), _ptr(gauge), _dims(L), n, float(kappa), int(dagger),
+    sc = np.empty(x.shape, dtype=np.complex128)
+    lib().oracle_wilson_full(_ptr(out), _ptr(x), _ptr(gauge), cp, _dims(L), n, float(kappa), int(dagger),
                              int(bool(antiperiodic_t)), _ptr(sc))
     return out
 
 
 def cgnr_full(b: np.ndarray, gauge: np.ndarray, L, kappa: float, tol: float = 1e-12, maxiter: int = 5000,
-              antiperiodic_t: bool = False):
+              antiperiodic_t: bool = False, clover=None):
     """Solve M x = b (full lattice, no preconditioning) by CGNR in FP64."""
     b = _c128(b)
     gauge = _c128(gauge)
+    cp, keep = _clover_ptr(clover)
     x = np.empty_like(b)
     res = ctypes.c_double()
-    it = lib().oracle_cgnr_full(_ptr(x), _ptr(b), _ptr(gauge), _dims(L), b.shape[-1], float(kappa),
+    it = lib().oracle_cgnr_full(_ptr(x), _ptr(b), _ptr(gauge), cp, _dims(L), b.shape[-1], float(kappa),
                                 int(bool(antiperiodic_t)), float(tol), int(maxiter), ctypes.byref(res))
     return x, it, res.value
 
 
 def true_residual(x: np.ndarray, b: np.ndarray, gauge: np.ndarray, L, kappa: float,
-                  antiperiodic_t: bool = False) -> float:
+                  antiperiodic_t: bool = False, clover=None) -> float:
     """|b - M x| / |b| in FP64 for a full eo field (2, Vh, 4, N)."""
     x = _c128(x)
     b = _c128(b)
     gauge = _c128(gauge)
-    return lib().oracle_true_residual(_ptr(x), _ptr(b), _ptr(gauge), _dims(L), b.shape[-1], float(kappa),
+    cp, keep = _clover_ptr(clover)
+    return lib().oracle_true_residual(_ptr(x), _ptr(b), _ptr(gauge), cp, _dims(L), b.shape[-1], float(kappa),
                                       int(bool(antiperiodic_t)))
 
 

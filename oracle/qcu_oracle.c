@@ -1,6 +1,7 @@
 /*
  * FP64 CPU oracle for the multi-right-hand-side even-odd Wilson dslash,
- * its layout conversions and the Wilson solve built on it.
+ * its layout conversions, the clover term and the (Wilson-clover) solve
+ * built on them.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
  * smoke check and the CPU-baseline leg of the benchmark load it.  The product
@@ -227,14 +228,54 @@ void oracle_eo_to_lex(double *lex, const double *eo, const int L[4], int ncomp) 
  *   out = in - kappa * D in,   in/out [2][Vh][4][N]
  * (kappa = 1/(2(4+m)) as at include/qcu_dirac.h:26; the reference never
  * applies it -- the solve path is new work, src/qcu.cu:173). */
-void oracle_wilson_full(double *out, const double *in, const double *gauge, const int L[4], int N, double kappa,
-                        int dagger, int antiperiodic_t, double *scratch /* [Vh][4][N] complex */) {
+/* Clover term of one parity (the reference only fixes its storage,
+ * include/basic_data/qcu_point.cuh:98-101: (Nc*Ns)^2/2 complex per site): per
+ * site two (2N x 2N) complex blocks, block 0 acting on spins 0, 1 and block 1
+ * on spins 2, 3 (the chirality blocks of the DeGrand-Rossi basis), row and
+ * column index = local spin * N + colour.  clover: [2][Vh][2][2N][2N] complex
+ * for both parities.  out = A_p in (dagger: A_p^dag in) for nrhs fields
+ * [nrhs][Vh][4][N]. */
+void oracle_clover_apply(double *out, const double *in, const double *clover, const int L[4], int N, int nrhs,
+                         int parity, int dagger) {
+  const int64_t Vh = (int64_t)L[0] * L[1] * L[2] * L[3] / 2;
+  const int n2 = 2 * N, blk = n2 * n2;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int r = 0; r < nrhs; r++)
+    for (int64_t i = 0; i < Vh; i++) {
+      const double *a = clover + (((int64_t)parity * Vh + i) * 2 * blk) * 2;
+      const double *v = in + (((int64_t)r * Vh + i) * NS * N) * 2;
+      double *o = out + (((int64_t)r * Vh + i) * NS * N) * 2;
+      for (int b = 0; b < 2; b++)
+        for (int row = 0; row < n2; row++) {
+          double re = 0, im = 0;
+          for (int col = 0; col < n2; col++) {
+            const int64_t e = dagger ? (int64_t)b * blk + col * n2 + row : (int64_t)b * blk + row * n2 + col;
+            const double mr = a[2 * e], mi = dagger ? -a[2 * e + 1] : a[2 * e + 1];
+            const double *x = v + ((int64_t)(2 * b) * N + col) * 2;
+            re += mr * x[0] - mi * x[1];
+            im += mr * x[1] + mi * x[0];
+          }
+          o[((int64_t)(2 * b) * N + row) * 2] = re;
+          o[((int64_t)(2 * b) * N + row) * 2 + 1] = im;
+        }
+    }
+}
+
+/* Full-lattice operator M = A - kappa D (A = 1 without a clover field, the
+ * Wilson operator), fields [2][Vh][4][N]; dagger: M^dag = A^dag - kappa D^dag.
+ * scratch: [2][Vh][4][N] complex. */
+void oracle_wilson_full(double *out, const double *in, const double *gauge, const double *clover, const int L[4],
+                        int N, double kappa, int dagger, int antiperiodic_t, double *scratch) {
   const int64_t Vh = (int64_t)L[0] * L[1] * L[2] * L[3] / 2;
   const int64_t n = Vh * NS * N * 2;
   for (int p = 0; p < 2; p++) {
     oracle_dslash(scratch, in + (int64_t)(1 - p) * n, gauge, L, N, 1, p, dagger, antiperiodic_t);
     double *o = out + (int64_t)p * n;
     const double *x = in + (int64_t)p * n;
+    if (clover) {
+      oracle_clover_apply(scratch + n, x, clover, L, N, 1, p, dagger);
+      x = scratch + n;
+    }
 #pragma omp parallel for schedule(static)
     for (int64_t k = 0; k < n; k++) o[k] = x[k] - kappa * scratch[k];
   }
@@ -250,23 +291,23 @@ static double dot_re(const double *a, const double *b, int64_t n) {
 /* CGNR on the full (unpreconditioned) Wilson system M x = b, one RHS, FP64:
  * an independent check of the even-odd preconditioned GPU solve.  Returns the
  * iteration count; *relres receives the true residual |b - M x| / |b|. */
-int oracle_cgnr_full(double *x, const double *b, const double *gauge, const int L[4], int N, double kappa,
-                     int antiperiodic_t, double tol, int maxiter, double *relres) {
+int oracle_cgnr_full(double *x, const double *b, const double *gauge, const double *clover, const int L[4], int N,
+                     double kappa, int antiperiodic_t, double tol, int maxiter, double *relres) {
   const int64_t Vh = (int64_t)L[0] * L[1] * L[2] * L[3] / 2;
   const int64_t n = 2 * Vh * NS * N * 2;
   double *r = malloc(sizeof(double) * n), *p = malloc(sizeof(double) * n), *Ap = malloc(sizeof(double) * n);
-  double *t = malloc(sizeof(double) * n), *sc = malloc(sizeof(double) * n / 2);
+  double *t = malloc(sizeof(double) * n), *sc = malloc(sizeof(double) * n);
   /* x = 0; r = M^dag b; p = r */
   memset(x, 0, sizeof(double) * n);
-  oracle_wilson_full(r, b, gauge, L, N, kappa, 1, antiperiodic_t, sc);
+  oracle_wilson_full(r, b, gauge, clover, L, N, kappa, 1, antiperiodic_t, sc);
   memcpy(p, r, sizeof(double) * n);
   double bb = dot_re(b, b, n);
   double rr = dot_re(r, r, n);
   int it = 0;
   for (; it < maxiter; it++) {
-    oracle_wilson_full(t, p, gauge, L, N, kappa, 0, antiperiodic_t, sc);
+    oracle_wilson_full(t, p, gauge, clover, L, N, kappa, 0, antiperiodic_t, sc);
     double pAp = dot_re(t, t, n);
-    oracle_wilson_full(Ap, t, gauge, L, N, kappa, 1, antiperiodic_t, sc);
+    oracle_wilson_full(Ap, t, gauge, clover, L, N, kappa, 1, antiperiodic_t, sc);
     double alpha = rr / pAp;
     for (int64_t k = 0; k < n; k++) {
       x[k] += alpha * p[k];
@@ -274,7 +315,7 @@ int oracle_cgnr_full(double *x, const double *b, const double *gauge, const int 
     }
     double rr_new = dot_re(r, r, n);
     /* stop on the true residual of M x = b */
-    oracle_wilson_full(t, x, gauge, L, N, kappa, 0, antiperiodic_t, sc);
+    oracle_wilson_full(t, x, gauge, clover, L, N, kappa, 0, antiperiodic_t, sc);
     double res = 0;
     for (int64_t k = 0; k < n; k++) res += (b[k] - t[k]) * (b[k] - t[k]);
     if (sqrt(res / bb) < tol) {
@@ -285,7 +326,7 @@ int oracle_cgnr_full(double *x, const double *b, const double *gauge, const int 
     rr = rr_new;
     for (int64_t k = 0; k < n; k++) p[k] = r[k] + beta * p[k];
   }
-  oracle_wilson_full(t, x, gauge, L, N, kappa, 0, antiperiodic_t, sc);
+  oracle_wilson_full(t, x, gauge, clover, L, N, kappa, 0, antiperiodic_t, sc);
   double res = 0;
   for (int64_t k = 0; k < n; k++) res += (b[k] - t[k]) * (b[k] - t[k]);
   *relres = sqrt(res / bb);
@@ -298,12 +339,12 @@ int oracle_cgnr_full(double *x, const double *b, const double *gauge, const int 
 }
 
 /* True residual |b - M x| / |b| of a full-lattice eo-split solution, one RHS. */
-double oracle_true_residual(const double *x, const double *b, const double *gauge, const int L[4], int N, double kappa,
-                            int antiperiodic_t) {
+double oracle_true_residual(const double *x, const double *b, const double *gauge, const double *clover,
+                            const int L[4], int N, double kappa, int antiperiodic_t) {
   const int64_t Vh = (int64_t)L[0] * L[1] * L[2] * L[3] / 2;
   const int64_t n = 2 * Vh * NS * N * 2;
-  double *t = malloc(sizeof(double) * n), *sc = malloc(sizeof(double) * n / 2);
-  oracle_wilson_full(t, x, gauge, L, N, kappa, 0, antiperiodic_t, sc);
+  double *t = malloc(sizeof(double) * n), *sc = malloc(sizeof(double) * n);
+  oracle_wilson_full(t, x, gauge, clover, L, N, kappa, 0, antiperiodic_t, sc);
   double res = 0, bb = 0;
   for (int64_t k = 0; k < n; k++) {
     res += (b[k] - t[k]) * (b[k] - t[k]);
