@@ -58,18 +58,21 @@ bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg) {
   return tma_plan(prec, N, A.geo, A.nrhs, cfg.R, cfg.tma, cfg.rcta, &T, &threads, &smem);
 }
 
-bool tc_runs(const DslashArgs& A, int prec, int N) {
+bool tc_runs(const DslashArgs& A, int prec, int N, int variant) {
   TcDslashArgs T;
-  return find_tc(prec, N) && A.in_norm && A.out_norm && tc_plan(prec, N, A.geo, A.nrhs, &T);
+  size_t smem = 0;
+  return find_tc(prec, N, variant) && A.in_norm && A.out_norm &&
+         (variant < 2 || ((uintptr_t)A.in % 16 == 0 && (uintptr_t)A.in_norm % 16 == 0)) &&
+         tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);
 }
 
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
   DslashConfig cfg = cfg_in;
-  if (cfg.tc && tc_runs(A, prec, N)) {
+  if (cfg.tc && tc_runs(A, prec, N, cfg.tc)) {
     DslashArgs B = A;
     B.af = (float)A.a;
     B.bf = (float)A.b;
-    find_tc(prec, N)(B, st);
+    find_tc(prec, N, cfg.tc)(B, st);
     QCU_CHECK_CUDA(cudaGetLastError());
     return;
   }

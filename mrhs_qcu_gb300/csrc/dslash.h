@@ -32,14 +32,14 @@ struct DslashConfig {
   int pk = 0;
   int tma = 0;   // > 0: the TMA-staged kernel (dslash_tma.cuh) with this many ring stages
   int rcta = 0;  // its RHS per tile (0: the largest that fits)
-  int tc = 0;    // 1: the tensor-core kernel (dslash_tc.cuh)
+  int tc = 0;    // tensor-core kernel (dslash_tc.cuh): 1 direct loads, 2 / 3 TMA ring of that depth
   int rc = 0;    // 1: SU(3) two-row links with the third row reconstructed (register kernel)
 };
 
 // whether the staged kernel of cfg can run these arguments
 bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg);
-// whether the tensor-core kernel can run these arguments
-bool tc_runs(const DslashArgs& A, int prec, int N);
+// whether the tensor-core kernel variant (1 direct, 2 / 3 TMA ring) can run these arguments
+bool tc_runs(const DslashArgs& A, int prec, int N, int variant = 1);
 
 // launch with an explicit configuration (throws if not compiled)
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st);

@@ -19,36 +19,54 @@ std::mutex& registry_mutex() {
 
 struct RegisterTc {
   RegisterTc() {
-    register_tc(PREC_BF16, 4, &launch_wilson_tc<4>);
-    register_tc(PREC_BF16, 5, &launch_wilson_tc<5>);
-    register_tc(PREC_BF16, 6, &launch_wilson_tc<6>);
-    register_tc(PREC_BF16, 7, &launch_wilson_tc<7>);
-    register_tc(PREC_BF16, 8, &launch_wilson_tc<8>);
+    register_tc(PREC_BF16, 4, 1, &launch_wilson_tc<4, 0>);
+    register_tc(PREC_BF16, 5, 1, &launch_wilson_tc<5, 0>);
+    register_tc(PREC_BF16, 6, 1, &launch_wilson_tc<6, 0>);
+    register_tc(PREC_BF16, 7, 1, &launch_wilson_tc<7, 0>);
+    register_tc(PREC_BF16, 8, 1, &launch_wilson_tc<8, 0>);
+    register_tc(PREC_BF16, 4, 2, &launch_wilson_tc<4, 2>);
+    register_tc(PREC_BF16, 6, 2, &launch_wilson_tc<6, 2>);
+    register_tc(PREC_BF16, 8, 2, &launch_wilson_tc<8, 2>);
+    register_tc(PREC_BF16, 4, 3, &launch_wilson_tc<4, 3>);
+    register_tc(PREC_BF16, 6, 3, &launch_wilson_tc<6, 3>);
+    register_tc(PREC_BF16, 8, 3, &launch_wilson_tc<8, 3>);
   }
 } register_tc_instances;
 
 }  // namespace
 
-bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, TcDslashArgs* T) {
-  if (prec != PREC_BF16 || N < 4 || N > 8 || nrhs < 1) return false;
+bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashArgs* T, size_t* smem) {
+  if (prec != PREC_BF16 || N < 4 || N > 8 || nrhs < 1 || nst < 0) return false;
   // 32-bit element offsets into the field and the gauge
   if ((int64_t)4 * N * geo.vh * nrhs >= (1ll << 32) || (int64_t)8 * N * N * geo.vh >= (1ll << 32)) return false;
   int rt = 64;
   while (nrhs % rt) rt--;
+  if (nst > 0 && (nrhs % 4 || rt % 4)) return false;  // 16-byte TMA rows
   const int64_t ntiles = (int64_t)geo.vh * (nrhs / rt);
   if (ntiles >= (1ll << 31)) return false;
   T->rt = rt;
   T->chunks = nrhs / rt;
   T->ntiles = (int)ntiles;
+  T->spin_bytes = T->norm_bytes = T->spin_stride = T->stage_bytes = 0;
+  *smem = tc::kSmemBytes;
+  if (nst > 0) {
+    T->spin_bytes = (uint32_t)(4 * N * rt * 4);
+    T->norm_bytes = (uint32_t)(rt * 4);
+    T->spin_stride = (T->spin_bytes + 127u) / 128u * 128u;
+    T->stage_bytes = T->spin_stride + (T->norm_bytes + 127u) / 128u * 128u;
+    *smem = (size_t)tc::kRingOffset + (size_t)nst * T->stage_bytes;
+  }
   return true;
 }
+
+int tc_ring_stages(int variant) { return variant >= 2 ? variant : 0; }
 
 // CTAs per SM from the kernel's registers and shared memory (the runtime's
 // occupancy query reports 1 for kernels that allocate tensor memory), capped
 // by the 512 tensor-memory columns at 32 per CTA.
-int tc_grid(const void* kernel, int ntiles) {
+int tc_grid(const void* kernel, int ntiles, size_t smem) {
   static std::mutex m;
-  static std::map<const void*, int> cache;
+  static std::map<std::pair<const void*, size_t>, int> cache;
   static int sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0;
   std::lock_guard<std::mutex> lk(m);
   if (!sms) {
@@ -60,17 +78,17 @@ int tc_grid(const void* kernel, int ntiles) {
     QCU_CHECK_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev));
     QCU_CHECK_CUDA(cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev));
   }
-  auto it = cache.find(kernel);
+  auto it = cache.find(std::make_pair(kernel, smem));
   int occ = 0;
   if (it == cache.end()) {
     cudaFuncAttributes fa;
     QCU_CHECK_CUDA(cudaFuncGetAttributes(&fa, kernel));
     const int regs = (fa.numRegs + 7) / 8 * 8;  // allocation granularity
-    const int by_smem = smem_sm / (tc::kSmemBytes + (int)fa.sharedSizeBytes + reserved);
+    const int by_smem = smem_sm / ((int)smem + (int)fa.sharedSizeBytes + reserved);
     const int by_regs = regs_sm / (std::max(regs, 1) * 128);
     const int by_thr = thr_sm / 128;
     occ = std::min(std::min(by_smem, by_regs), std::min(by_thr, 16));
-    cache[kernel] = occ;
+    cache[std::make_pair(kernel, smem)] = occ;
   } else {
     occ = it->second;
   }
@@ -78,14 +96,14 @@ int tc_grid(const void* kernel, int ntiles) {
   return std::min(ntiles, occ * sms);
 }
 
-void register_tc(int prec, int N, TcLauncher fn) {
+void register_tc(int prec, int N, int variant, TcLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[prec * 16 + N] = fn;
+  registry()[(prec * 16 + N) * 8 + variant] = fn;
 }
 
-TcLauncher find_tc(int prec, int N) {
+TcLauncher find_tc(int prec, int N, int variant) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find(prec * 16 + N);
+  auto it = registry().find((prec * 16 + N) * 8 + variant);
   return it == registry().end() ? nullptr : it->second;
 }
 

@@ -41,12 +41,18 @@ struct TcDslashArgs {
   int chunks;  // nrhs / rt
   int ntiles;  // vh * chunks
   int* err;    // set to 1 when a wait times out
+  // TMA-fed variant: ring stage = the neighbour site's [4N][rt] spinor block + its [rt] scales
+  uint32_t spin_bytes = 0, norm_bytes = 0, spin_stride = 0, stage_bytes = 0;
 };
 
 namespace tc {
 
 constexpr int kSetBytes = 9216;  // A 4096, A' 4096, B 512, B' 512
 constexpr int kSmemBytes = 2 * kSetBytes + 64;
+// TMA-fed variant: the stage ring starts 128-byte aligned after the operands
+// and the barriers (operand barriers at +0, +8; tensor-memory slot at +16;
+// ring barriers at +24 + 8 s)
+constexpr int kRingOffset = 2 * kSetBytes + 128;
 
 // shared-memory matrix descriptor: K-major, no swizzle; lbo = byte stride of
 // core matrices along K, sbo = along M (N for B); bits 46-48 = 0b001
@@ -101,9 +107,42 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
 
 }  // namespace tc
 
-template <int N>
-__global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ TcDslashArgs T) {
+// neighbour (half-lattice index) of `site` for hop d (mu = d / 2, forward for even d)
+__device__ __forceinline__ uint32_t tc_neighbour(const DslashArgs& A, uint32_t site, int d) {
+  uint32_t rest, xh, y, z, t, rest2;
+  A.geo.div_hx.divmod(site, rest, xh);
+  A.geo.div_y.divmod(rest, rest2, y);
+  A.geo.div_z.divmod(rest2, t, z);
+  const uint32_t hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3], p = A.parity;
+  const uint32_t eo = (y + z + t) & 1u;
+  const bool fwd = (d & 1) == 0;
+  switch (d >> 1) {
+    case 0:
+      return fwd ? ((eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site)
+                 : ((eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site);
+    case 1:
+      return fwd ? ((y == Ly - 1) ? site - (Ly - 1) * hx : site + hx) : ((y == 0) ? site + (Ly - 1) * hx : site - hx);
+    case 2: {
+      const uint32_t pl = A.geo.plane;
+      return fwd ? ((z == Lz - 1) ? site - (Lz - 1) * pl : site + pl) : ((z == 0) ? site + (Lz - 1) * pl : site - pl);
+    }
+    default: {
+      const uint32_t cb = A.geo.cube;
+      return fwd ? ((t == Lt - 1) ? site - (Lt - 1) * cb : site + cb) : ((t == 0) ? site + (Lt - 1) * cb : site - cb);
+    }
+  }
+}
+
+// NST = 0: the projection reads the neighbour spinors straight from global
+// memory; NST > 0: thread 0 streams them (and their scales) with one TMA box
+// per hop into a ring of NST shared-memory stages, NST - 1 hops ahead.  The
+// CTA barrier of every hop orders the reads of a stage before its refill.
+template <int N, int NST>
+__global__ void __launch_bounds__(128)
+    wilson_tc_kernel(const __grid_constant__ TcDslashArgs T, const __grid_constant__ CUtensorMap map_in,
+                     const __grid_constant__ CUtensorMap map_norm) {
   static_assert(N >= 2 && N <= 8, "K = 2N must fit one K = 16 MMA step");
+  static_assert(NST >= 0 && NST <= 4, "ring stages");
   using namespace detail;
   using S = Store<PREC_BF16>;
   using E = typename S::elem;
@@ -115,9 +154,11 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
   const uint32_t smem0 = tma::smem_u32(smem);
   const int tid = threadIdx.x, warp = tid >> 5;
 
+  const uint32_t ring_bar0 = bar0 + 24;  // NST ring barriers
   if (tid == 0) {
     tma::mbar_init(bar0, 1);
     tma::mbar_init(bar0 + 8, 1);
+    for (int st = 0; st < NST; st++) tma::mbar_init(ring_bar0 + 8 * st, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -153,6 +194,26 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
 
   uint32_t q = 0;  // hops issued so far (operand buffer = q & 1)
   bool failed = false;
+  // TMA ring (thread 0): hop qq of this CTA -> its stage, issued NST - 1 hops ahead
+  uint32_t issued = 0;
+  auto issue = [&](uint32_t qq) {
+    if constexpr (NST > 0) {
+      const int tile = (int)blockIdx.x + (int)(qq >> 3) * (int)gridDim.x;
+      if (tile >= T.ntiles) return;
+      const uint32_t st_site = (uint32_t)(tile / T.chunks), st_chunk = (uint32_t)(tile % T.chunks);
+      const uint32_t nbq = tc_neighbour(A, st_site, (int)(qq & 7u));
+      const uint32_t stage = qq % NST, bar = ring_bar0 + 8 * stage;
+      const uint32_t dst = smem0 + tc::kRingOffset + stage * T.stage_bytes;
+      tma::mbar_expect_tx(bar, T.spin_bytes + T.norm_bytes);
+      tma::load_3d(dst, &map_in, (int)(st_chunk * T.rt), (int)nbq, 0, bar);
+      tma::load_2d(dst + T.spin_stride, &map_norm, (int)(st_chunk * T.rt), (int)nbq, bar);
+      issued = qq + 1;
+    }
+  };
+  if constexpr (NST > 0) {
+    if (tid == 0)
+      for (uint32_t qq = 0; qq + 1 < (uint32_t)NST; qq++) issue(qq);
+  }
   for (int tile = blockIdx.x; tile < T.ntiles && !failed; tile += gridDim.x) {
     const uint32_t site = (uint32_t)(tile / T.chunks), chunk = (uint32_t)(tile % T.chunks);
     const uint32_t rhs = chunk * (uint32_t)T.rt + (uint32_t)r;
@@ -173,6 +234,16 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
       // operand buffer b is free once the MMAs of hop q - 2 have completed
       bool ok = true;
       if (q >= 2) ok = tma::mbar_poll(bar0 + 8 * b, ((q >> 1) - 1) & 1u, T.err);
+      const unsigned char* stage_p = nullptr;
+      if constexpr (NST > 0) {
+        // refill the stage hop q - 1 read (all threads have passed its barrier), then wait for hop q's
+        if (tid == 0) {
+          tc::fence_async_smem();  // the stage's generic reads (ordered by the last barrier) before the refill
+          issue(q + NST - 1);
+        }
+        ok = ok && tma::mbar_poll(ring_bar0 + 8 * (q % NST), (q / NST) & 1u, T.err);
+        stage_p = smem + tc::kRingOffset + (q % NST) * T.stage_bytes;
+      }
       uint32_t nb;
       float bc = 1.f;
       if constexpr (mu == 0) {
@@ -194,16 +265,29 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
       if (ok && row_live) {
         // projected row u of RHS rhs, scaled by bc * norm(nb, rhs); A row word c = (Re h_c, Im h_c)
         const int up = (mu < 2) ? 3 - u : (u ^ 2);
-        const float scale = bc * __ldg(A.in_norm + (nb * nrhs + rhs));
+        float nrm;
+        const E *xp, *yp;
+        uint32_t astride;  // element stride between colours
+        if constexpr (NST > 0) {
+          // stage: [4N][rt] spinor components, then [rt] scales
+          nrm = reinterpret_cast<const float*>(stage_p + T.spin_stride)[r];
+          xp = reinterpret_cast<const E*>(stage_p) + (uint32_t)(u * N) * T.rt + r;
+          yp = reinterpret_cast<const E*>(stage_p) + (uint32_t)(up * N) * T.rt + r;
+          astride = (uint32_t)T.rt;
+        } else {
+          nrm = __ldg(A.in_norm + (nb * nrhs + rhs));
+          xp = in + ((uint32_t)(u * N) * cs + nb * nrhs + rhs);
+          yp = in + ((uint32_t)(up * N) * cs + nb * nrhs + rhs);
+          astride = cs;
+        }
+        const float scale = bc * nrm;
         const float ks = s * (float)gsign(mu, u) * scale;
-        const E* xp = in + ((uint32_t)(u * N) * cs + nb * nrhs + rhs);
-        const E* yp = in + ((uint32_t)(up * N) * cs + nb * nrhs + rhs);
         uint32_t va[8];
 #pragma unroll
         for (int a = 0; a < 8; a++) {
           if (a < N) {
-            const float2 x = S::to_c(__ldg(xp + (uint32_t)a * cs));
-            const float2 yv = S::to_c(__ldg(yp + (uint32_t)a * cs));
+            const float2 x = S::to_c(NST > 0 ? xp[(uint32_t)a * astride] : __ldg(xp + (uint32_t)a * astride));
+            const float2 yv = S::to_c(NST > 0 ? yp[(uint32_t)a * astride] : __ldg(yp + (uint32_t)a * astride));
             float hr, hi;
             if constexpr (imag) {
               hr = fmaf(-ks, yv.y, scale * x.x);
@@ -327,6 +411,11 @@ __global__ void __launch_bounds__(128) wilson_tc_kernel(const __grid_constant__ 
     // let the MMAs in flight finish before the tensor memory is released (bounded)
     const uint32_t ql = q - 1;
     tma::mbar_poll(bar0 + 8 * (ql & 1u), (ql >> 1) & 1u, T.err);
+  }
+  if constexpr (NST > 0) {
+    // copies still in flight land before the CTA's shared memory is released (bounded)
+    if (failed && tid == 0)
+      for (uint32_t qq = q; qq < issued; qq++) tma::mbar_poll(ring_bar0 + 8 * (qq % NST), (qq / NST) & 1u, T.err);
   }
   tc::fence_before();
   __syncthreads();

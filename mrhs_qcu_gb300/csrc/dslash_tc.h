@@ -2,32 +2,52 @@
 // registry.
 #pragma once
 
+#include <cstring>
+
 #include "dslash.h"
 #include "dslash_tc.cuh"
 #include "dslash_tma.h"
 
 namespace qcu {
 
-// Tile plan for (precision, N, geometry, nrhs): false when the tensor-core
-// kernel cannot run these arguments (BF16 storage and N = 4..8 only).
-bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, TcDslashArgs* T);
-int tc_grid(const void* kernel, int ntiles);
+// Tile plan for (precision, N, geometry, nrhs) and ring depth nst (0: no
+// ring): false when the tensor-core kernel cannot run these arguments (BF16
+// storage and N = 4..8 only; the ring also needs nrhs and the tile's RHS
+// count to be multiples of 4 for its TMA boxes).  *smem: dynamic shared bytes.
+bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashArgs* T, size_t* smem);
+int tc_grid(const void* kernel, int ntiles, size_t smem);
 
-template <int N>
+template <int N, int NST>
 void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
   TcDslashArgs T;
-  QCU_REQUIRE(tc_plan(PREC_BF16, N, A.geo, A.nrhs, &T), QCU_ERR_UNSUPPORTED,
+  size_t smem = 0;
+  QCU_REQUIRE(tc_plan(PREC_BF16, N, A.geo, A.nrhs, NST, &T, &smem), QCU_ERR_UNSUPPORTED,
               "tensor-core dslash: arguments outside the kernel's limits");
   T.A = A;
   T.err = tma_error_flag();
-  const void* k = reinterpret_cast<const void*>(&wilson_tc_kernel<N>);
-  const int grid = tc_grid(k, T.ntiles);
-  wilson_tc_kernel<N><<<grid, 128, tc::kSmemBytes, st>>>(T);
+  CUtensorMap mi, mn;
+  if constexpr (NST > 0) {
+    tma_encode_field(&mi, A.in, 4, A.nrhs, A.geo.vh, 4 * N, T.rt, 1);
+    tma_encode_norm(&mn, A.in_norm, A.nrhs, A.geo.vh, T.rt, 1);
+  } else {
+    memset(&mi, 0, sizeof(mi));  // not read
+    memset(&mn, 0, sizeof(mn));
+  }
+  const void* k = reinterpret_cast<const void*>(&wilson_tc_kernel<N, NST>);
+  static size_t smem_set = 0;
+  if (smem > 48 * 1024 && smem > smem_set) {
+    QCU_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_set = smem;
+  }
+  const int grid = tc_grid(k, T.ntiles, smem);
+  wilson_tc_kernel<N, NST><<<grid, 128, smem, st>>>(T, mi, mn);
   tma_note_launch();
 }
 
+// variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
-void register_tc(int prec, int N, TcLauncher fn);
-TcLauncher find_tc(int prec, int N);
+void register_tc(int prec, int N, int variant, TcLauncher fn);
+TcLauncher find_tc(int prec, int N, int variant = 1);
+int tc_ring_stages(int variant);
 
 }  // namespace qcu

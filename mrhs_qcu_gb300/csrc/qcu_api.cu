@@ -454,7 +454,8 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
     for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0);
-    if (qcu::find_tc(precision, nColors)) put(1, 0, 0, -1, 0);
+    for (int v = 1; v <= 3; v++)
+      if (qcu::find_tc(precision, nColors, v)) put(1, 0, 0, -v, 0);
     *count = n;
   });
 }
@@ -492,7 +493,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (block) *block = c.block;
     if (min_blocks) *min_blocks = c.minb;
     if (packed) *packed = c.pk;
-    if (stages) *stages = c.tc ? -1 : c.tma;
+    if (stages) *stages = c.tc ? -c.tc : c.tma;
     if (recon) *recon = c.rc;
   });
 }

@@ -89,7 +89,7 @@ DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
     const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc,
                            &c.rc);
     if (got < 8) c.rc = 0;
-    const bool tensor = got >= 7 && c.tc == 1 && find_tc(prec, N);
+    const bool tensor = got >= 7 && c.tc >= 1 && find_tc(prec, N, c.tc);
     const bool staged = !tensor && got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 &&
                         find_tma(prec, N, c.R, c.tma);
     const bool plain = !tensor && got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
@@ -197,9 +197,10 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
     }
   }
   // the tensor-core kernel, where these arguments fit it
-  if (tc_runs(A, prec, N)) {
+  for (int variant = 1; variant <= 3; variant++) {
+    if (!tc_runs(A, prec, N, variant)) continue;
     DslashConfig c;
-    c.tc = 1;
+    c.tc = variant;
     launch_dslash(A, prec, N, c, st);  // warm-up
     QCU_CHECK_CUDA(cudaEventRecord(e0, st));
     const int reps = 3;
