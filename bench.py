@@ -55,9 +55,10 @@ METRIC = "dslash site\u00b7RHS/s & % HBM roofline; mixed vs FP64 solve time @1e-
 def bytes_per_site_rhs(prec: int, n: int, nrhs: int) -> float:
     """Compulsory bytes per output site per RHS: 8 links (N^2 complex each,
     amortised over the RHS) + one input and one output spinor (4N complex)
-    + the per-(site, RHS) FP32 scale of 16-bit storage, read and written."""
+    + the per-(site, RHS) FP32 scale of FP16 storage, read and written
+    (BF16 fields are unscaled)."""
     c = {2: 16, 1: 8, 0: 4, 4: 4}[prec]
-    nn = 4 if prec in (0, 4) else 0
+    nn = 4 if prec == 0 else 0
     return 8 * n * n * c / nrhs + 2 * (4 * n * c + nn)
 
 
@@ -303,7 +304,8 @@ def run_gpu(args):
             "traffic": traffic.get("dram_bytes_per_launch_tma" if stages > 0 else
                                    "dram_bytes_per_launch_rc" if recon else "dram_bytes_per_launch_reg")
             if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1 and n == NC) else None,
-            "kernel": ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
+            "kernel": ("wilson_tcs_kernel<N=%d,stages=%d> (tcgen05)" % (n, -stages - 2)) if stages <= -4 else
+                      ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
                       ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
                       ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
                        % (pname, n, R, minb, pk, recon, block)),
@@ -490,7 +492,10 @@ def colors_bench(torch, Q, peak, fma):
         for p, pname, kernel, pin in ((1, "fp32", "cuda_core", None), (4, "bf16", "cuda_core", "2,64,1,0"),
                                       (4, "bf16", "tensor_core", "1,0,0,0,0,0,1"),
                                       (4, "bf16", "tensor_core_tma2", "1,0,0,0,0,0,2"),
-                                      (4, "bf16", "tensor_core_tma3", "1,0,0,0,0,0,3")):
+                                      (4, "bf16", "tensor_core_tma3", "1,0,0,0,0,0,3"),
+                                      (4, "bf16", "tensor_core_spinor2", "1,0,0,0,0,0,4"),
+                                      (4, "bf16", "tensor_core_spinor3", "1,0,0,0,0,0,5"),
+                                      (4, "bf16", "tensor_core_spinor4", "1,0,0,0,0,0,6")):
             for nr in (16, 32, 64):
                 if pin:
                     os.environ["QCU_DSLASH_CONFIG"] = pin

@@ -13,8 +13,9 @@
  * Internal MRHS field of one parity (for the session lattice and N):
  *   data  [4N][Vh][nrhs] complex in the field precision (component-major,
  *         RHS innermost)
- *   norm  [Vh][nrhs] float, present only for 16-bit storage; stored values
- *         are component / norm(site, rhs)
+ *   norm  [Vh][nrhs] float, present only for FP16 storage; stored values
+ *         are component / norm(site, rhs).  BF16 has the FP32 exponent range
+ *         and is stored unscaled (no norm array; norm pointers are ignored).
  * Sizes come from qcuFieldBytes.  Buffers must be 16-byte aligned.
  */
 #pragma once

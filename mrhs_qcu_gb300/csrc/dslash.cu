@@ -61,8 +61,13 @@ bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg) {
 bool tc_runs(const DslashArgs& A, int prec, int N, int variant) {
   TcDslashArgs T;
   size_t smem = 0;
-  return find_tc(prec, N, variant) && A.in_norm && A.out_norm &&
-         (variant < 2 || ((uintptr_t)A.in % 16 == 0 && (uintptr_t)A.in_norm % 16 == 0)) &&
+  if (!find_tc(prec, N, variant)) return false;
+  if (variant >= 4) {
+    TcsDslashArgs T4;
+    CUtensorMap m;
+    return tcs_plan(A, N, tc_ring_stages(variant), &T4, &smem, &m);
+  }
+  return (variant < 2 || (uintptr_t)A.in % 16 == 0) &&
          tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);
 }
 

@@ -47,24 +47,42 @@ bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashAr
   T->rt = rt;
   T->chunks = nrhs / rt;
   T->ntiles = (int)ntiles;
-  T->spin_bytes = T->norm_bytes = T->spin_stride = T->stage_bytes = 0;
+  T->spin_bytes = T->stage_bytes = 0;
   *smem = tc::kSmemBytes;
   if (nst > 0) {
     T->spin_bytes = (uint32_t)(4 * N * rt * 4);
-    T->norm_bytes = (uint32_t)(rt * 4);
-    T->spin_stride = (T->spin_bytes + 127u) / 128u * 128u;
-    T->stage_bytes = T->spin_stride + (T->norm_bytes + 127u) / 128u * 128u;
+    T->stage_bytes = (T->spin_bytes + 127u) / 128u * 128u;
     *smem = (size_t)tc::kRingOffset + (size_t)nst * T->stage_bytes;
   }
   return true;
 }
 
-int tc_ring_stages(int variant) { return variant >= 2 ? variant : 0; }
+int tc_ring_stages(int variant) { return variant >= 4 ? variant - 2 : variant >= 2 ? variant : 0; }
+
+bool tcs_plan(const DslashArgs& A, int N, int nst, TcsDslashArgs* T, size_t* smem, CUtensorMap* map_in) {
+  const Geometry& geo = A.geo;
+  const int nrhs = A.nrhs;
+  if (N < 2 || N > 8 || nst < 2 || nst > 4 || nrhs < 1 || nrhs % 4 || geo.vh % 4) return false;
+  if (((uintptr_t)A.in | (uintptr_t)A.gauge) % 16) return false;
+  // 32-bit BF16 scalar offsets into the field (2 per complex) and element offsets into the gauge
+  if ((int64_t)8 * N * geo.vh * nrhs >= (1ll << 32) || (int64_t)8 * N * N * geo.vh >= (1ll << 32)) return false;
+  int rt = 64;
+  while (nrhs % rt || rt % 4) rt--;
+  const int64_t ntiles = (int64_t)geo.vh * (nrhs / rt);
+  if (ntiles >= (1ll << 31)) return false;
+  if (!tma_encode_field_swizzled(map_in, A.in, nrhs, geo.vh, N)) return false;
+  T->rt = rt;
+  T->chunks = nrhs / rt;
+  T->ntiles = (int)ntiles;
+  T->halves = rt > 32 ? 2 : 1;
+  *smem = tcs::smem_bytes(nst);
+  return true;
+}
 
 // CTAs per SM from the kernel's registers and shared memory (the runtime's
 // occupancy query reports 1 for kernels that allocate tensor memory), capped
-// by the 512 tensor-memory columns at 32 per CTA.
-int tc_grid(const void* kernel, int ntiles, size_t smem) {
+// by the 512 tensor-memory columns.
+int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols) {
   static std::mutex m;
   static std::map<std::pair<const void*, size_t>, int> cache;
   static int sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0;
@@ -87,7 +105,7 @@ int tc_grid(const void* kernel, int ntiles, size_t smem) {
     const int by_smem = smem_sm / ((int)smem + (int)fa.sharedSizeBytes + reserved);
     const int by_regs = regs_sm / (std::max(regs, 1) * 128);
     const int by_thr = thr_sm / 128;
-    occ = std::min(std::min(by_smem, by_regs), std::min(by_thr, 16));
+    occ = std::min(std::min(by_smem, by_regs), std::min(by_thr, 512 / std::max(tmem_cols, 32)));
     cache[std::make_pair(kernel, smem)] = occ;
   } else {
     occ = it->second;

@@ -12,11 +12,11 @@
 // and B' = B times the +-i of the imaginary gamma rows (mu = x, z).  Both
 // accumulate over the eight hops in tensor memory (FP32, 2 x 16 columns of
 // 128 lanes), so the CUDA cores only project (h = psi_u + k psi_perm(u),
-// scaled by the neighbour's storage scale and the boundary sign), convert to
+// times the boundary sign), convert to
 // BF16 and write the operands; the N x N complex multiply runs on the tensor
 // pipe, with the link operand built once per hop and used by all RHS of the
 // tile.  The epilogue reads the accumulators back (tcgen05.ld), applies the
-// xpay / per-RHS a, and writes BF16 with per-(site, RHS) scales.
+// xpay / per-RHS a, and writes BF16 (BF16 fields are stored unscaled).
 //
 // CTA = 128 threads, thread m = 2 r + u owns row m (TMEM lane m).  Operands
 // are double buffered in shared memory; an mbarrier per buffer signals
@@ -41,8 +41,8 @@ struct TcDslashArgs {
   int chunks;  // nrhs / rt
   int ntiles;  // vh * chunks
   int* err;    // set to 1 when a wait times out
-  // TMA-fed variant: ring stage = the neighbour site's [4N][rt] spinor block + its [rt] scales
-  uint32_t spin_bytes = 0, norm_bytes = 0, spin_stride = 0, stage_bytes = 0;
+  // TMA-fed variant: ring stage = the neighbour site's [4N][rt] spinor block
+  uint32_t spin_bytes = 0, stage_bytes = 0;
 };
 
 namespace tc {
@@ -134,13 +134,12 @@ __device__ __forceinline__ uint32_t tc_neighbour(const DslashArgs& A, uint32_t s
 }
 
 // NST = 0: the projection reads the neighbour spinors straight from global
-// memory; NST > 0: thread 0 streams them (and their scales) with one TMA box
+// memory; NST > 0: thread 0 streams them with one TMA box
 // per hop into a ring of NST shared-memory stages, NST - 1 hops ahead.  The
 // CTA barrier of every hop orders the reads of a stage before its refill.
 template <int N, int NST>
 __global__ void __launch_bounds__(128)
-    wilson_tc_kernel(const __grid_constant__ TcDslashArgs T, const __grid_constant__ CUtensorMap map_in,
-                     const __grid_constant__ CUtensorMap map_norm) {
+    wilson_tc_kernel(const __grid_constant__ TcDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
   static_assert(N >= 2 && N <= 8, "K = 2N must fit one K = 16 MMA step");
   static_assert(NST >= 0 && NST <= 4, "ring stages");
   using namespace detail;
@@ -204,9 +203,8 @@ __global__ void __launch_bounds__(128)
       const uint32_t nbq = tc_neighbour(A, st_site, (int)(qq & 7u));
       const uint32_t stage = qq % NST, bar = ring_bar0 + 8 * stage;
       const uint32_t dst = smem0 + tc::kRingOffset + stage * T.stage_bytes;
-      tma::mbar_expect_tx(bar, T.spin_bytes + T.norm_bytes);
+      tma::mbar_expect_tx(bar, T.spin_bytes);
       tma::load_3d(dst, &map_in, (int)(st_chunk * T.rt), (int)nbq, 0, bar);
-      tma::load_2d(dst + T.spin_stride, &map_norm, (int)(st_chunk * T.rt), (int)nbq, bar);
       issued = qq + 1;
     }
   };
@@ -263,24 +261,21 @@ __global__ void __launch_bounds__(128)
       unsigned char* set = smem + b * tc::kSetBytes;
 
       if (ok && row_live) {
-        // projected row u of RHS rhs, scaled by bc * norm(nb, rhs); A row word c = (Re h_c, Im h_c)
+        // projected row u of RHS rhs, times the boundary sign bc; A row word c = (Re h_c, Im h_c)
         const int up = (mu < 2) ? 3 - u : (u ^ 2);
-        float nrm;
         const E *xp, *yp;
         uint32_t astride;  // element stride between colours
         if constexpr (NST > 0) {
-          // stage: [4N][rt] spinor components, then [rt] scales
-          nrm = reinterpret_cast<const float*>(stage_p + T.spin_stride)[r];
+          // stage: [4N][rt] spinor components
           xp = reinterpret_cast<const E*>(stage_p) + (uint32_t)(u * N) * T.rt + r;
           yp = reinterpret_cast<const E*>(stage_p) + (uint32_t)(up * N) * T.rt + r;
           astride = (uint32_t)T.rt;
         } else {
-          nrm = __ldg(A.in_norm + (nb * nrhs + rhs));
           xp = in + ((uint32_t)(u * N) * cs + nb * nrhs + rhs);
           yp = in + ((uint32_t)(up * N) * cs + nb * nrhs + rhs);
           astride = cs;
         }
-        const float scale = bc * nrm;
+        const float scale = bc;
         const float ks = s * (float)gsign(mu, u) * scale;
         uint32_t va[8];
 #pragma unroll
@@ -370,11 +365,10 @@ __global__ void __launch_bounds__(128)
       o[0][a] = up_v[a];
       o[1][a] = lo_v[a];
     }
-    float mx = 0.f;
     if (row_live) {
       const float ca = A.a_rhs_f ? A.a_rhs_f[rhs] : A.af;
       const E* __restrict__ xin = static_cast<const E*>(A.x);
-      const float xs = xin ? A.bf * A.x_norm[site * nrhs + rhs] : 0.f;
+      const float xs = A.bf;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const uint32_t sp = (uint32_t)(u + 2 * h);
@@ -388,21 +382,17 @@ __global__ void __launch_bounds__(128)
           }
           o[h][2 * a] = re;
           o[h][2 * a + 1] = im;
-          mx = fmaxf(mx, fmaxf(fabsf(re), fabsf(im)));
         }
       }
     }
-    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));  // the other two spins of this RHS (lane m ^ 1)
     if (row_live && (!A.mask || A.mask[rhs] != 0)) {
-      const float inv = mx > 0.f ? 1.f / mx : 0.f;
       E* __restrict__ out = static_cast<E*>(A.out);
-      if (u == 0) A.out_norm[site * nrhs + rhs] = mx;
 #pragma unroll
       for (int h = 0; h < 2; h++) {
         const uint32_t sp = (uint32_t)(u + 2 * h);
 #pragma unroll
         for (int a = 0; a < N; a++)
-          out[(sp * N + a) * cs + site * nrhs + rhs] = S::from_c(make_float2(o[h][2 * a] * inv, o[h][2 * a + 1] * inv));
+          out[(sp * N + a) * cs + site * nrhs + rhs] = S::from_c(make_float2(o[h][2 * a], o[h][2 * a + 1]));
       }
     }
   }

@@ -6,6 +6,7 @@
 
 #include "dslash.h"
 #include "dslash_tc.cuh"
+#include "dslash_tcs.cuh"
 #include "dslash_tma.h"
 
 namespace qcu {
@@ -15,7 +16,36 @@ namespace qcu {
 // storage and N = 4..8 only; the ring also needs nrhs and the tile's RHS
 // count to be multiples of 4 for its TMA boxes).  *smem: dynamic shared bytes.
 bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashArgs* T, size_t* smem);
-int tc_grid(const void* kernel, int ntiles, size_t smem);
+// grid of a persistent tensor-core kernel: CTAs per SM from registers and
+// shared memory, capped so that their tensor memory (tmem_cols each) fits
+int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols = 32);
+
+// Tile plan of the spinor-operand kernel (dslash_tcs.cuh) with a ring of nst
+// stages; false when it cannot run these arguments (BF16, N = 2..8, nrhs a
+// multiple of 4, Vh a multiple of 4, 16-byte aligned field and gauge, 32-bit
+// element offsets, and a field map the driver accepts).
+bool tcs_plan(const DslashArgs& A, int N, int nst, TcsDslashArgs* T, size_t* smem, CUtensorMap* map_in);
+
+template <int N, int NST>
+void launch_wilson_tcs(const DslashArgs& A, cudaStream_t st) {
+  TcsDslashArgs T;
+  size_t smem = 0;
+  CUtensorMap mi, mg;
+  QCU_REQUIRE(tcs_plan(A, N, NST, &T, &smem, &mi), QCU_ERR_UNSUPPORTED,
+              "tensor-core dslash: arguments outside the kernel's limits");
+  T.A = A;
+  T.err = tma_error_flag();
+  tma_encode_gauge(&mg, A.gauge, 4, A.geo.vh, N * N, 4);
+  const void* k = reinterpret_cast<const void*>(&wilson_tcs_kernel<N, NST>);
+  static size_t smem_set = 0;
+  if (smem > 48 * 1024 && smem > smem_set) {
+    QCU_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    smem_set = smem;
+  }
+  const int grid = tc_grid(k, T.ntiles, smem, (int)tcs::kTmemCols);
+  wilson_tcs_kernel<N, NST><<<grid, 128, smem, st>>>(T, mi, mg);
+  tma_note_launch();
+}
 
 template <int N, int NST>
 void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
@@ -25,14 +55,11 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
               "tensor-core dslash: arguments outside the kernel's limits");
   T.A = A;
   T.err = tma_error_flag();
-  CUtensorMap mi, mn;
-  if constexpr (NST > 0) {
+  CUtensorMap mi;
+  if constexpr (NST > 0)
     tma_encode_field(&mi, A.in, 4, A.nrhs, A.geo.vh, 4 * N, T.rt, 1);
-    tma_encode_norm(&mn, A.in_norm, A.nrhs, A.geo.vh, T.rt, 1);
-  } else {
+  else
     memset(&mi, 0, sizeof(mi));  // not read
-    memset(&mn, 0, sizeof(mn));
-  }
   const void* k = reinterpret_cast<const void*>(&wilson_tc_kernel<N, NST>);
   static size_t smem_set = 0;
   if (smem > 48 * 1024 && smem > smem_set) {
@@ -40,11 +67,13 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
     smem_set = smem;
   }
   const int grid = tc_grid(k, T.ntiles, smem);
-  wilson_tc_kernel<N, NST><<<grid, 128, smem, st>>>(T, mi, mn);
+  wilson_tc_kernel<N, NST><<<grid, 128, smem, st>>>(T, mi);
   tma_note_launch();
 }
 
-// variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages
+// variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages (projected
+// half-spinor operands, dslash_tc.cuh); 4 / 5 / 6 = the spinor-operand kernel
+// (dslash_tcs.cuh) with 2 / 3 / 4 ring stages
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
 void register_tc(int prec, int N, int variant, TcLauncher fn);
 TcLauncher find_tc(int prec, int N, int variant = 1);

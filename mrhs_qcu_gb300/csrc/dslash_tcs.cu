@@ -1,0 +1,27 @@
+// Instances of the spinor-operand tensor-core dslash (dslash_tcs.cuh):
+// tensor-core variants 4 / 5 / 6 = ring depth 2 / 3 / 4, BF16, N = 3..8.
+#include "dslash_tc.h"
+
+namespace qcu {
+namespace {
+
+template <int N>
+void register_n() {
+  register_tc(PREC_BF16, N, 4, &launch_wilson_tcs<N, 2>);
+  register_tc(PREC_BF16, N, 5, &launch_wilson_tcs<N, 3>);
+  register_tc(PREC_BF16, N, 6, &launch_wilson_tcs<N, 4>);
+}
+
+struct RegisterTcs {
+  RegisterTcs() {
+    register_n<3>();
+    register_n<4>();
+    register_n<5>();
+    register_n<6>();
+    register_n<7>();
+    register_n<8>();
+  }
+} register_tcs_instances;
+
+}  // namespace
+}  // namespace qcu

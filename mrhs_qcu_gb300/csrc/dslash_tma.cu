@@ -96,6 +96,17 @@ void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int n
   encode(m, ptr, dims, strides, box);
 }
 
+bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N) {
+  const cuuint64_t cs = (cuuint64_t)vh * nrhs * 4;  // component stride, bytes
+  const cuuint64_t dims[4] = {(cuuint64_t)nrhs, (cuuint64_t)N, 4, (cuuint64_t)vh};
+  const cuuint64_t strides[3] = {cs, (cuuint64_t)N * cs, (cuuint64_t)nrhs * 4};
+  const cuuint32_t box[4] = {32, 8, 4, 1};
+  const cuuint32_t es[4] = {1, 1, 1, 1};
+  return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rcta, int hx) {
   const cuuint64_t dims[3] = {(cuuint64_t)nrhs, (cuuint64_t)vh, 1};
   const cuuint64_t strides[2] = {(cuuint64_t)nrhs * 4, (cuuint64_t)vh * nrhs * 4};
@@ -106,7 +117,7 @@ void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rct
 bool tma_plan(int prec, int N, const Geometry& geo, int nrhs, int R, int nst, int rcta, TmaDslashArgs* T,
               int* threads, size_t* smem) {
   if (N < 1 || nst < 1) return false;
-  const bool norm = prec_is16(prec);
+  const bool norm = prec_has_norm(prec);
   const int E = prec_complex_bytes(prec);
   const int hx = geo.hx;
   // TMA: 16-byte aligned row starts and strides, box extents <= 256

@@ -292,7 +292,7 @@ int qcuPackFermions(void* dst, void* dst_norm, void* const* src, int nrhs, int s
     QCU_REQUIRE(nrhs >= 1 && nrhs <= qcu::QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
     QCU_REQUIRE(src_mode >= 0 && src_mode <= 2, QCU_ERR_INVALID_ARGUMENT, "bad source mode");
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
-    QCU_REQUIRE(!qcu::prec_is16(precision) || dst_norm, QCU_ERR_INVALID_ARGUMENT, "16-bit fields need a norm array");
+    QCU_REQUIRE(!qcu::prec_has_norm(precision) || dst_norm, QCU_ERR_INVALID_ARGUMENT, "FP16 fields need a norm array");
     qcu::PtrArray p{};
     for (int r = 0; r < nrhs; r++) p.p[r] = src[r];
     qcu::pack_fermions(precision, s.N, p, src_mode, parity, dst, static_cast<float*>(dst_norm), s.geo, nrhs,
@@ -369,9 +369,9 @@ int qcuDslashXpayMRHS(void* out, void* out_norm, const void* in, const void* in_
     QCU_REQUIRE(out != in, QCU_ERR_INVALID_ARGUMENT, "in-place dslash is not supported");
     QCU_REQUIRE(((uintptr_t)out | (uintptr_t)in | (uintptr_t)x) % 16 == 0, QCU_ERR_INVALID_ARGUMENT,
                 "fields must be 16-byte aligned");
-    const bool h = qcu::prec_is16(precision);
+    const bool h = qcu::prec_has_norm(precision);
     QCU_REQUIRE(!h || (out_norm && in_norm && (!x || x_norm)), QCU_ERR_INVALID_ARGUMENT,
-                "16-bit fields need norm arrays");
+                "FP16 fields need norm arrays");
     qcu::FieldView fo, fi, fx;
     fo.data = out;
     fo.norm = static_cast<float*>(out_norm);
@@ -402,8 +402,8 @@ int qcuCloverMRHS(void* out, void* out_norm, const void* in, const void* in_norm
     QCU_REQUIRE(out && in && out != in, QCU_ERR_INVALID_ARGUMENT, "null or in-place field");
     QCU_REQUIRE(((uintptr_t)out | (uintptr_t)in) % 16 == 0, QCU_ERR_INVALID_ARGUMENT,
                 "fields must be 16-byte aligned");
-    QCU_REQUIRE(!qcu::prec_is16(precision) || (out_norm && in_norm), QCU_ERR_INVALID_ARGUMENT,
-                "16-bit fields need norm arrays");
+    QCU_REQUIRE(!qcu::prec_has_norm(precision) || (out_norm && in_norm), QCU_ERR_INVALID_ARGUMENT,
+                "FP16 fields need norm arrays");
     qcu::FieldView fo, fi;
     fo.data = out;
     fo.norm = static_cast<float*>(out_norm);
@@ -454,7 +454,7 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
     for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0);
-    for (int v = 1; v <= 3; v++)
+    for (int v = 1; v <= 6; v++)
       if (qcu::find_tc(precision, nColors, v)) put(1, 0, 0, -v, 0);
     *count = n;
   });

@@ -28,6 +28,9 @@ enum Prec : int { PREC_HALF = 0, PREC_SINGLE = 1, PREC_DOUBLE = 2, PREC_BF16 = 4
 
 inline bool prec_valid(int p) { return p == PREC_HALF || p == PREC_SINGLE || p == PREC_DOUBLE || p == PREC_BF16; }
 inline bool prec_is16(int p) { return p == PREC_HALF || p == PREC_BF16; }
+// FP16 fields carry a per-(site, RHS) FP32 scale; BF16 has the FP32 exponent
+// range, so its fields are stored unscaled
+inline bool prec_has_norm(int p) { return p == PREC_HALF; }
 inline int prec_complex_bytes(int p) { return p == PREC_DOUBLE ? 16 : (p == PREC_SINGLE ? 8 : 4); }
 inline const char* prec_name(int p) {
   switch (p) {
@@ -155,7 +158,7 @@ template <> struct Store<PREC_HALF> {
 template <> struct Store<PREC_BF16> {
   using elem = __nv_bfloat162;
   using real = float;
-  static constexpr bool has_norm = true;
+  static constexpr bool has_norm = false;
   __device__ __forceinline__ static float2 to_c(__nv_bfloat162 v) { return __bfloat1622float2(v); }
   __device__ __forceinline__ static __nv_bfloat162 from_c(float2 v) { return __float22bfloat162_rn(v); }
 };

@@ -197,7 +197,7 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
     }
   }
   // the tensor-core kernel, where these arguments fit it
-  for (int variant = 1; variant <= 3; variant++) {
+  for (int variant = 1; variant <= 6; variant++) {
     if (!tc_runs(A, prec, N, variant)) continue;
     DslashConfig c;
     c.tc = variant;
@@ -363,7 +363,7 @@ FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {
   f.prec = prec;
   f.nrhs = nrhs;
   f.data = ws.get(name, field_bytes(prec, nrhs));
-  if (prec_is16(prec)) f.norm = static_cast<float*>(ws.get(name + ".norm", norm_bytes(prec, nrhs)));
+  if (prec_has_norm(prec)) f.norm = static_cast<float*>(ws.get(name + ".norm", norm_bytes(prec, nrhs)));
   return f;
 }
 

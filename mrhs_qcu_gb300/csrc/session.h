@@ -165,7 +165,7 @@ class Session {
   // ---- fields ------------------------------------------------------------
   size_t field_elems(int nrhs) const { return (size_t)geo.vh * 4 * N * nrhs; }
   size_t field_bytes(int prec, int nrhs) const { return field_elems(nrhs) * prec_complex_bytes(prec); }
-  size_t norm_bytes(int prec, int nrhs) const { return prec_is16(prec) ? (size_t)geo.vh * nrhs * 4 : 0; }
+  size_t norm_bytes(int prec, int nrhs) const { return prec_has_norm(prec) ? (size_t)geo.vh * nrhs * 4 : 0; }
   FieldView alloc_field(const std::string& name, int prec, int nrhs);
 
   // out = a * D in + b * x  (x.data may be null), on the library stream.

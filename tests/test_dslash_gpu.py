@@ -110,18 +110,22 @@ def test_reconstructed_links_only_for_su3_fields(cuda, qcu_lib, prec):
         del os.environ["QCU_DSLASH_CONFIG"]
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3])
-@pytest.mark.parametrize("n,nrhs", [(4, 16), (8, 16), (6, 24), (8, 64), (5, 128)])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("n,nrhs", [(4, 16), (8, 16), (6, 24), (8, 64), (5, 128), (3, 32), (7, 36), (8, 8)])
 def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
-    """The tcgen05 kernel (BF16 storage and operands, FP32 accumulation in
+    """The tcgen05 kernels (BF16 storage and operands, FP32 accumulation in
     tensor memory) against the FP64 oracle: both parities and dagger flags,
     antiperiodic t, RHS counts that fill the 128 MMA rows, leave them partly
-    empty, or take two tiles."""
+    empty, take two tiles, or end inside the second 32-RHS box.  Variants 1-3
+    are the projected half-spinor kernel (N >= 4; the TMA ring for N = 4, 6,
+    8), 4-6 the spinor-operand kernel with 2-4 ring stages."""
     L = (4, 4, 4, 8)
     g = S.random_gauge(L, n, seed=90 + n)
     psi = S.random_fermions(L, n, nrhs, seed=91)
-    if variant > 1 and n == 5:
-        pytest.skip("the TMA-ring variants are compiled for N = 4, 6, 8")
+    if variant <= 3 and n == 3:
+        pytest.skip("the projected kernel is compiled for N >= 4")
+    if variant in (2, 3) and n in (5, 7):
+        pytest.skip("the projected kernel's TMA ring is compiled for N = 4, 6, 8")
     os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
     try:
         for parity, dag in ((0, 0), (1, 1), (1, 0)):
@@ -132,8 +136,9 @@ def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
         del os.environ["QCU_DSLASH_CONFIG"]
 
 
-def test_tensor_core_xpay_resident(cuda, qcu_lib):
-    """xpay epilogue and per-site scales of the tensor-core kernel on resident fields."""
+@pytest.mark.parametrize("variant", [1, 4])
+def test_tensor_core_xpay_resident(cuda, qcu_lib, variant):
+    """xpay epilogue of the tensor-core kernels on resident BF16 fields."""
     torch, Q = cuda, qcu_lib
     L, n, nrhs = (4, 4, 4, 8), 4, 16
     g = S.random_gauge(L, n, seed=95)
@@ -150,7 +155,7 @@ def test_tensor_core_xpay_resident(cuda, qcu_lib):
     Q.pack_fermions(bufs[0].data_ptr(), norms[0].data_ptr(), ptrs, Q.QCU_SRC_EO_FULL, 0, 4)
     Q.pack_fermions(bufs[1].data_ptr(), norms[1].data_ptr(), ptrs, Q.QCU_SRC_EO_FULL, 1, 4)
     a, b = 0.37, -1.25
-    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,1"
+    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
     try:
         Q.dslash_xpay_mrhs(bufs[2].data_ptr(), norms[2].data_ptr(), bufs[0].data_ptr(), norms[0].data_ptr(),
                            bufs[1].data_ptr(), norms[1].data_ptr(), nrhs, 1, 0, 4, a, b)

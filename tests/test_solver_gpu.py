@@ -156,3 +156,27 @@ def test_gamma5_hermiticity_of_schur_operator(cuda, qcu_lib):
     lhs = np.vdot(y, mhat(x, 0))
     rhs = np.vdot(mhat(y, 1), x)
     assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("variant", [1, 4])
+def test_bicgstab_bf16_tensor_core_masks(cuda, qcu_lib, variant):
+    """BiCGStab with BF16 inner dslash on the tensor cores (SU(4), 16 RHS, one
+    source 1e-4 times smaller, one zero) to 1e-8, checked by the oracle's
+    FP64 true residual: the masked tensor-core epilogue inside the solver."""
+    import os
+    torch, Q = cuda, qcu_lib
+    L, n, kappa, tol, nrhs = (4, 4, 4, 8), 4, 0.11, 1e-8, 16
+    g, _ = setup(torch, Q, L, n, 250)
+    b = S.random_fermions(L, n, nrhs, seed=251, parities=2)
+    b[1] *= 1e-4
+    b[2] = 0.0
+    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
+    try:
+        x, p = solve(torch, Q, b, kappa=kappa, tol=tol, inner_precision=4, solver=Q.QCU_SOLVER_BICGSTAB)
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
+    for r in range(nrhs):
+        assert p.converged[r] == 1
+        if r != 2:
+            assert O.true_residual(x[r], b[r], g, L, kappa, antiperiodic_t=True) < 2 * tol
+    assert not np.any(x[2])

@@ -97,3 +97,96 @@ def test_tensor_core_operands_reproduce_the_hop(n, parity, dagger, ap):
     got = tc_hop(psi, g, L, parity, dagger, ap)
     ref = O.dslash(psi, g, L, parity, dagger, ap)
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-13
+
+
+# ---- spinor-operand formulation (csrc/dslash_tcs.cuh) -------------------------
+#
+# A[m][k]: m = 2 r + ri (RHS r, Re / Im part ri), k = 8 s' + b (input spin s',
+# colour b padded to 8) -- the neighbour block exactly as it sits in memory.
+# B[k][n]: n = 32 part + 8 s + a (part 0 / 1 = Re / Im of K_hop), the real
+# split of K_hop^T, K_hop[(s, a)][(s', b)] = bc P[s][s'] W[a][b], built in
+# 16-byte chunks (fixed n, 8 consecutive k = one input spin) as signed copies
+# of the rows Re W[a][.] / Im W[a][.].  D = sum over hops of A B; the
+# epilogue forms Re out = D[(r,Re)][ReK] - D[(r,Im)][ImK] and
+# Im out = D[(r,Im)][ReK] + D[(r,Re)][ImK].
+
+def chunk_code(mu, fwd, s, g, dagger, bc):
+    """(source part swap, sign) of the B chunk for output spin s, input spin
+    g, or None for a zero chunk -- the selection the kernel makes."""
+    perm = 3 - s if mu < 2 else s ^ 2
+    if g == s:
+        return False, bc  # z = bc
+    if g != perm:
+        return None
+    sg = (-1 if fwd else 1) * gsign(mu, s) * (-1 if dagger else 1) * bc
+    return mu in (0, 2), sg  # z = sg * (i if imaginary gamma row)
+
+
+def tcs_hop(psi, g, L, p, dagger, antiperiodic):
+    nrhs, vh, _, N = psi.shape
+    hx, Ly, Lz, Lt = L[0] // 2, L[1], L[2], L[3]
+    plane, cube = hx * Ly, hx * Ly * Lz
+    out = np.zeros_like(psi)
+    for site in range(vh):
+        xh, rest = site % hx, site // hx
+        y, rest2 = rest % Ly, rest // Ly
+        z, t = rest2 % Lz, rest2 // Lz
+        eo = (y + z + t) & 1
+        d = np.zeros((2 * nrhs, 64))
+        for hop in range(8):
+            mu, fwd, bc = hop >> 1, (hop & 1) == 0, 1.0
+            if mu == 0:
+                if fwd:
+                    nb = (site - (hx - 1) if xh == hx - 1 else site + 1) if eo != p else site
+                else:
+                    nb = (site + (hx - 1) if xh == 0 else site - 1) if eo == p else site
+            elif mu == 1:
+                nb = (site - (Ly - 1) * hx if y == Ly - 1 else site + hx) if fwd else \
+                     (site + (Ly - 1) * hx if y == 0 else site - hx)
+            elif mu == 2:
+                nb = (site - (Lz - 1) * plane if z == Lz - 1 else site + plane) if fwd else \
+                     (site + (Lz - 1) * plane if z == 0 else site - plane)
+            else:
+                nb = (site - (Lt - 1) * cube if t == Lt - 1 else site + cube) if fwd else \
+                     (site + (Lt - 1) * cube if t == 0 else site - cube)
+                if antiperiodic and (t == Lt - 1 if fwd else t == 0):
+                    bc = -1.0
+            u = g[mu, p, site] if fwd else g[mu, 1 - p, nb]
+            w = u if fwd else np.conj(u.T)
+            # rows Re W[a][.], Im W[a][.], padded to 8 x 8
+            wrow = np.zeros((2, 8, 8))
+            wrow[0, :N, :N], wrow[1, :N, :N] = w.real, w.imag
+            a_op = np.zeros((2 * nrhs, 32))
+            for r in range(nrhs):
+                for sp in range(4):
+                    a_op[2 * r, 8 * sp:8 * sp + N] = psi[r, nb, sp].real
+                    a_op[2 * r + 1, 8 * sp:8 * sp + N] = psi[r, nb, sp].imag
+            b_op = np.zeros((32, 64))
+            for c in range(256):  # the kernel's chunk numbering
+                a, gs, s, part = c & 7, (c >> 3) & 3, (c >> 5) & 3, c >> 7
+                code = chunk_code(mu, fwd, s, gs, dagger, bc)
+                if code is None:
+                    continue
+                imag, sg = code
+                src = part ^ int(imag)
+                # z = sg (real): part -> sg * row part; z = sg * i: Re -> -sg Im W, Im -> +sg Re W
+                neg = (sg < 0) if not imag else ((sg > 0) if part == 0 else (sg < 0))
+                b_op[8 * gs:8 * gs + 8, 32 * part + 8 * s + a] = (-1 if neg else 1) * wrow[src, a]
+            d += a_op @ b_op
+        for r in range(nrhs):
+            re = d[2 * r, 0:32] - d[2 * r + 1, 32:64]
+            im = d[2 * r + 1, 0:32] + d[2 * r, 32:64]
+            for sp in range(4):
+                out[r, site, sp] = re[8 * sp:8 * sp + N] + 1j * im[8 * sp:8 * sp + N]
+    return out
+
+
+@pytest.mark.parametrize("n", [3, 4, 8])
+@pytest.mark.parametrize("parity,dagger,ap", [(0, 0, True), (1, 1, True), (1, 0, False), (0, 1, False)])
+def test_spinor_operand_formulation_reproduces_the_hop(n, parity, dagger, ap):
+    L = (4, 2, 2, 4)
+    g = S.random_gauge(L, n, seed=13)
+    psi = S.random_fermions(L, n, 3, seed=14)
+    got = tcs_hop(psi, g, L, parity, dagger, ap)
+    ref = O.dslash(psi, g, L, parity, dagger, ap)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-13
