@@ -65,7 +65,7 @@ bool tc_runs(const DslashArgs& A, int prec, int N, int variant) {
   if (variant >= 4) {
     TcsDslashArgs T4;
     CUtensorMap m;
-    return tcs_plan(A, N, tc_ring_stages(variant), &T4, &smem, &m);
+    return tcs_plan(A, N, &T4, &m);
   }
   return (variant < 2 || (uintptr_t)A.in % 16 == 0) &&
          tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);

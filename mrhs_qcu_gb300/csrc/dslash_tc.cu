@@ -57,13 +57,13 @@ bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashAr
   return true;
 }
 
-int tc_ring_stages(int variant) { return variant >= 4 ? variant - 2 : variant >= 2 ? variant : 0; }
+int tc_ring_stages(int variant) { return variant >= 2 && variant <= 3 ? variant : 0; }
 
-bool tcs_plan(const DslashArgs& A, int N, int nst, TcsDslashArgs* T, size_t* smem, CUtensorMap* map_in) {
+bool tcs_plan(const DslashArgs& A, int N, TcsDslashArgs* T, CUtensorMap* map_in) {
   const Geometry& geo = A.geo;
   const int nrhs = A.nrhs;
-  if (N < 2 || N > 8 || nst < 2 || nst > 4 || nrhs < 1 || nrhs % 4 || geo.vh % 4) return false;
-  if (((uintptr_t)A.in | (uintptr_t)A.gauge) % 16) return false;
+  if (N < 2 || N > 8 || nrhs < 1 || nrhs % 4 || !A.gauge_tc) return false;
+  if (((uintptr_t)A.in | (uintptr_t)A.gauge_tc) % 16) return false;
   // 32-bit BF16 scalar offsets into the field (2 per complex) and element offsets into the gauge
   if ((int64_t)8 * N * geo.vh * nrhs >= (1ll << 32) || (int64_t)8 * N * N * geo.vh >= (1ll << 32)) return false;
   int rt = 64;
@@ -75,14 +75,13 @@ bool tcs_plan(const DslashArgs& A, int N, int nst, TcsDslashArgs* T, size_t* sme
   T->chunks = nrhs / rt;
   T->ntiles = (int)ntiles;
   T->halves = rt > 32 ? 2 : 1;
-  *smem = tcs::smem_bytes(nst);
   return true;
 }
 
 // CTAs per SM from the kernel's registers and shared memory (the runtime's
 // occupancy query reports 1 for kernels that allocate tensor memory), capped
 // by the 512 tensor-memory columns.
-int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols) {
+int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols, int threads) {
   static std::mutex m;
   static std::map<std::pair<const void*, size_t>, int> cache;
   static int sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0, thr_sm = 0;
@@ -103,8 +102,8 @@ int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols) {
     QCU_CHECK_CUDA(cudaFuncGetAttributes(&fa, kernel));
     const int regs = (fa.numRegs + 7) / 8 * 8;  // allocation granularity
     const int by_smem = smem_sm / ((int)smem + (int)fa.sharedSizeBytes + reserved);
-    const int by_regs = regs_sm / (std::max(regs, 1) * 128);
-    const int by_thr = thr_sm / 128;
+    const int by_regs = regs_sm / (std::max(regs, 1) * threads);
+    const int by_thr = thr_sm / threads;
     occ = std::min(std::min(by_smem, by_regs), std::min(by_thr, 512 / std::max(tmem_cols, 32)));
     cache[std::make_pair(kernel, smem)] = occ;
   } else {

@@ -18,32 +18,36 @@ namespace qcu {
 bool tc_plan(int prec, int N, const Geometry& geo, int nrhs, int nst, TcDslashArgs* T, size_t* smem);
 // grid of a persistent tensor-core kernel: CTAs per SM from registers and
 // shared memory, capped so that their tensor memory (tmem_cols each) fits
-int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols = 32);
+int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols = 32, int threads = 128);
 
-// Tile plan of the spinor-operand kernel (dslash_tcs.cuh) with a ring of nst
-// stages; false when it cannot run these arguments (BF16, N = 2..8, nrhs a
-// multiple of 4, Vh a multiple of 4, 16-byte aligned field and gauge, 32-bit
-// element offsets, and a field map the driver accepts).
-bool tcs_plan(const DslashArgs& A, int N, int nst, TcsDslashArgs* T, size_t* smem, CUtensorMap* map_in);
+// Tile plan of the spinor-operand kernel (dslash_tcs.cuh); false when it
+// cannot run these arguments (BF16, N = 2..8, nrhs a multiple of 4, the
+// site-major links present, 16-byte aligned field and links, 32-bit element
+// offsets, and a field map the driver accepts).
+bool tcs_plan(const DslashArgs& A, int N, TcsDslashArgs* T, CUtensorMap* map_in);
 
-template <int N, int NST>
+// ring depths of the spinor-operand variants 4, 5, 6: (TMA stages, B buffers)
+constexpr int tcs_stages(int variant) { return variant == 5 ? 6 : variant == 6 ? 3 : 4; }
+constexpr int tcs_bbufs(int variant) { return variant == 6 ? 2 : 3; }
+
+template <int N, int V>
 void launch_wilson_tcs(const DslashArgs& A, cudaStream_t st) {
+  constexpr int NST = tcs_stages(V), NB = tcs_bbufs(V);
   TcsDslashArgs T;
-  size_t smem = 0;
-  CUtensorMap mi, mg;
-  QCU_REQUIRE(tcs_plan(A, N, NST, &T, &smem, &mi), QCU_ERR_UNSUPPORTED,
+  CUtensorMap mi;
+  QCU_REQUIRE(tcs_plan(A, N, &T, &mi), QCU_ERR_UNSUPPORTED,
               "tensor-core dslash: arguments outside the kernel's limits");
   T.A = A;
   T.err = tma_error_flag();
-  tma_encode_gauge(&mg, A.gauge, 4, A.geo.vh, N * N, 4);
-  const void* k = reinterpret_cast<const void*>(&wilson_tcs_kernel<N, NST>);
+  const size_t smem = tcs::smem_bytes(NST, NB);
+  const void* k = reinterpret_cast<const void*>(&wilson_tcs_kernel<N, NST, NB>);
   static size_t smem_set = 0;
   if (smem > 48 * 1024 && smem > smem_set) {
     QCU_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     smem_set = smem;
   }
-  const int grid = tc_grid(k, T.ntiles, smem, (int)tcs::kTmemCols);
-  wilson_tcs_kernel<N, NST><<<grid, 128, smem, st>>>(T, mi, mg);
+  const int grid = tc_grid(k, T.ntiles, smem, (int)tcs::kTmemCols, tcs::kThreads);
+  wilson_tcs_kernel<N, NST, NB><<<grid, tcs::kThreads, smem, st>>>(T, mi);
   tma_note_launch();
 }
 
@@ -73,7 +77,7 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
 
 // variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages (projected
 // half-spinor operands, dslash_tc.cuh); 4 / 5 / 6 = the spinor-operand kernel
-// (dslash_tcs.cuh) with 2 / 3 / 4 ring stages
+// (dslash_tcs.cuh) with (TMA stages, B buffers) = (4, 3) / (6, 3) / (3, 2)
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
 void register_tc(int prec, int N, int variant, TcLauncher fn);
 TcLauncher find_tc(int prec, int N, int variant = 1);

@@ -1,5 +1,5 @@
 // Instances of the spinor-operand tensor-core dslash (dslash_tcs.cuh):
-// tensor-core variants 4 / 5 / 6 = ring depth 2 / 3 / 4, BF16, N = 3..8.
+// tensor-core variants 4 / 5 / 6 (ring depths in dslash_tc.h), BF16, N = 3..8.
 #include "dslash_tc.h"
 
 namespace qcu {
@@ -7,9 +7,9 @@ namespace {
 
 template <int N>
 void register_n() {
-  register_tc(PREC_BF16, N, 4, &launch_wilson_tcs<N, 2>);
-  register_tc(PREC_BF16, N, 5, &launch_wilson_tcs<N, 3>);
-  register_tc(PREC_BF16, N, 6, &launch_wilson_tcs<N, 4>);
+  register_tc(PREC_BF16, N, 4, &launch_wilson_tcs<N, 4>);
+  register_tc(PREC_BF16, N, 5, &launch_wilson_tcs<N, 5>);
+  register_tc(PREC_BF16, N, 6, &launch_wilson_tcs<N, 6>);
 }
 
 struct RegisterTcs {

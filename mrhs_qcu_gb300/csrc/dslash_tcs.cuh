@@ -26,13 +26,25 @@
 // projection, conversion and operand stores of every spinor element; the
 // tensor pipe has that work to spare.
 //
-// CTA = 128 threads; thread m owns TMEM lane m (= A row m) in the epilogue.
-// Ring of NST stages, each the A block of one hop (two 4 KB halves of 32 RHS)
-// and the hop's link box ([N*N][4 sites], 16-byte aligned site start);
-// thread 0 issues the TMA NST - 1 hops ahead and refills a stage once the MMA
-// that read it has committed.  B is double buffered.  Every wait is bounded;
-// a timeout sets *err, the CTA agrees to stop (__syncthreads_or), drains its
-// MMAs and copies in flight (bounded), frees its tensor memory and returns.
+// Persistent, warp-specialized CTA of 320 threads; the roles hand work to
+// each other through mbarriers only:
+//   warps 0-3  B builders: per hop, the link rows W (threads 32 .. 32+N*N-1,
+//              one element each of the hop's link, copied with the A block)
+//              and the 4 KB B operand into a ring of NB buffers; one named
+//              barrier per hop between the two steps
+//   warp 4     MMA issuer (one thread): two MMAs per hop into one of two
+//              tensor-memory accumulators; commits free the B buffer and the
+//              TMA stage, and hand a finished tile to the epilogue
+//   warp 5     TMA producer (one thread): per hop, the neighbour's A block
+//              (one or two boxes of 32 RHS) and the link (one bulk copy from
+//              the site-major BF16 links, layout.h gauge_site_major_bf16)
+//              into a ring of NST stages, as far ahead as the ring allows
+//   warps 6-9  epilogue: tensor memory -> Re/Im combination -> global, one
+//              tile behind the MMAs (double-buffered accumulator)
+// Every wait is bounded (about 1 s); a timeout sets *err and a shared abort
+// flag that every other wait checks, so all roles leave their loops; the
+// MMA issuer then waits (bounded) for its MMAs, the producer for its copies,
+// and the CTA frees its tensor memory and returns.
 #pragma once
 
 #include <type_traits>
@@ -54,17 +66,22 @@ namespace tcs {
 
 constexpr uint32_t kHalfBytes = 4096;               // 4 spins x 8 colours x 128 B
 constexpr uint32_t kABytes = 2 * kHalfBytes;        // M = 128 rows
-constexpr uint32_t kLinkBytes = 1024;               // [N*N <= 64][4 sites] x 4 B
-constexpr uint32_t kStageBytes = kABytes + kLinkBytes;  // 9 KB, keeps every A block 1024-byte aligned
+constexpr uint32_t kLinkBytes = 1024;               // one site-major link (<= 256 B), 1 KB keeps stages aligned
+constexpr uint32_t kStageBytes = kABytes + kLinkBytes;
 constexpr uint32_t kBBytes = 4096;                  // 64 (n) x 32 (k) BF16, K-major
-constexpr uint32_t kTmemCols = 64;
+constexpr uint32_t kTmemCols = 128;  // two accumulators of 64 columns
 
-// offsets from the 1024-byte aligned base of dynamic shared memory
+// offsets from the 1024-byte aligned base of dynamic shared memory: TMA
+// stages, B buffers, two W-row buffers, barriers
 __host__ __device__ constexpr uint32_t b_off(int nst) { return (uint32_t)nst * kStageBytes; }
-__host__ __device__ constexpr uint32_t w_off(int nst) { return b_off(nst) + 2 * kBBytes; }
-__host__ __device__ constexpr uint32_t bar_off(int nst) { return w_off(nst) + 256; }
+__host__ __device__ constexpr uint32_t w_off(int nst, int nb) { return b_off(nst) + (uint32_t)nb * kBBytes; }
+__host__ __device__ constexpr uint32_t bar_off(int nst, int nb) { return w_off(nst, nb) + 512; }
+// barriers: ring_full[nst], ring_empty[nst], b_full[nb], b_empty[nb],
+// tmem_full[2], tmem_empty[2], drain; then the tensor-memory slot and the abort flag
+__host__ __device__ constexpr uint32_t slot_off(int nst, int nb) { return bar_off(nst, nb) + 8u * (2 * nst + 2 * nb + 5); }
 // + 1024 bytes to align the base
-__host__ __device__ constexpr uint32_t smem_bytes(int nst) { return bar_off(nst) + 128 + 1024; }
+__host__ __device__ constexpr uint32_t smem_bytes(int nst, int nb) { return slot_off(nst, nb) + 16 + 1024; }
+constexpr int kThreads = 320;
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, A MN-major (bit
 // 15), B K-major, N = 64, M = 128
@@ -86,27 +103,107 @@ __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
                : "memory");
 }
 
-// 4-D tiled TMA load into shared memory, completion counted on bar
+// 1-D bulk copy global -> shared (16-byte aligned, size a multiple of 16), completion counted on bar
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// coordinates of an output site, decomposed once per tile
+struct SiteCoords {
+  uint32_t site, xh, y, z, t, eo;
+  __device__ __forceinline__ SiteCoords(const DslashArgs& A, uint32_t s) : site(s) {
+    uint32_t rest, rest2;
+    A.geo.div_hx.divmod(s, rest, xh);
+    A.geo.div_y.divmod(rest, rest2, y);
+    A.geo.div_z.divmod(rest2, t, z);
+    eo = (y + z + t) & 1u;
+  }
+  // neighbour for hop d = 2 mu + (backward ? 1 : 0) (d known at compile time)
+  __device__ __forceinline__ uint32_t nb(const DslashArgs& A, int d) const {
+    const uint32_t hx = A.geo.hx, p = A.parity;
+    switch (d) {
+      case 0: return (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+      case 1: return (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+      case 2: return (y == A.geo.L[1] - 1) ? site - (A.geo.L[1] - 1) * hx : site + hx;
+      case 3: return (y == 0) ? site + (A.geo.L[1] - 1) * hx : site - hx;
+      case 4: return (z == A.geo.L[2] - 1) ? site - (A.geo.L[2] - 1) * A.geo.plane : site + A.geo.plane;
+      case 5: return (z == 0) ? site + (A.geo.L[2] - 1) * A.geo.plane : site - A.geo.plane;
+      case 6: return (t == A.geo.L[3] - 1) ? site - (A.geo.L[3] - 1) * A.geo.cube : site + A.geo.cube;
+      default: return (t == 0) ? site + (A.geo.L[3] - 1) * A.geo.cube : site - A.geo.cube;
+    }
+  }
+};
+
+// L2 policy that keeps lines resident (each neighbour block is read by the
+// eight sites around it, a short while apart)
+__device__ __forceinline__ uint64_t evict_last_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// 4-D tiled TMA load into shared memory with an L2 cache policy, completion counted on bar
 __device__ __forceinline__ void load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
-                                        uint32_t bar) {
+                                        uint32_t bar, uint64_t policy) {
   asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
-      "%5}], [%6];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, "
+      "{%2, %3, %4, %5}], [%6], %7;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar), "l"(policy)
       : "memory");
+}
+
+// Bounded wait for the phase of `bar` with the given parity that also gives
+// up when another role has set the CTA's abort flag; a timeout (about 1 s)
+// sets *err and the abort flag.  Waiting threads are suspended in try_wait
+// (suspend-time hint) rather than spinning.
+__device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, volatile int* abort_flag) {
+  uint32_t ok = 0;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  if (ok) return true;
+  const uint64_t t0 = tma::now_ns();
+  for (uint32_t i = 1;; i++) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity), "r"(20000u)
+        : "memory");
+    if (ok) return true;
+    if (*abort_flag) return false;
+    if ((i & 15u) == 0 && tma::now_ns() - t0 > 1000000000ull) {
+      atomicExch(err, 1);
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+
+// named barrier `id` over `count` threads with an OR reduction of `pred`
+__device__ __forceinline__ bool bar_or(int id, int count, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
 }
 
 }  // namespace tcs
 
 // map_in: the input field as [site][spin 4][colour N][RHS] of 4-byte complex
-// BF16, box (32 RHS, 8 colours, 4 spins, 1 site), 128-byte swizzle.
-// map_gauge: the gauge as [(mu, parity) 8][N*N][Vh] of 4-byte elements, box (4 sites, N*N, 1).
-template <int N, int NST>
-__global__ void __launch_bounds__(128)
-    wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in,
-                      const __grid_constant__ CUtensorMap map_gauge) {
+// BF16, box (32 RHS, 8 colours, 4 spins, 1 site), 128-byte swizzle.  The
+// links come from A.gauge_tc (site-major BF16, one bulk copy per hop).
+template <int N, int NST, int NB>
+__global__ void __launch_bounds__(tcs::kThreads, 4)
+    wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
   static_assert(N >= 2 && N <= 8, "colours are padded to 8");
-  static_assert(NST >= 2 && NST <= 4, "ring stages");
+  static_assert(NST >= 2 && NST <= 8 && NB >= 2 && NB <= 4, "ring depths");
   using namespace detail;
   const DslashArgs& A = T.A;
   extern __shared__ unsigned char smem_raw[];
@@ -114,114 +211,96 @@ __global__ void __launch_bounds__(128)
   const uint32_t raw0 = tma::smem_u32(smem_raw);
   const uint32_t smem0 = (raw0 + 1023u) & ~1023u;
   unsigned char* smem = smem_raw + (smem0 - raw0);
-  const uint32_t bar_mma = smem0 + tcs::bar_off(NST);  // [2]: the MMAs of hops using B buffer 0 / 1
-  const uint32_t bar_ring = bar_mma + 16;               // [NST]: a stage's TMA landed
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + tcs::bar_off(NST) + 64);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t ring_full = smem0 + tcs::bar_off(NST, NB);
+  const uint32_t ring_empty = ring_full + 8 * NST;
+  const uint32_t b_full = ring_empty + 8 * NST;
+  const uint32_t b_empty = b_full + 8 * NB;
+  const uint32_t tmem_full = b_empty + 8 * NB;
+  const uint32_t tmem_empty = tmem_full + 16;
+  const uint32_t drain = tmem_empty + 16;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + tcs::slot_off(NST, NB));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + tcs::slot_off(NST, NB) + 8);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
-    tma::mbar_init(bar_mma, 1);
-    tma::mbar_init(bar_mma + 8, 1);
-    for (int st = 0; st < NST; st++) tma::mbar_init(bar_ring + 8 * st, 1);
+    for (int i = 0; i < NST; i++) {
+      tma::mbar_init(ring_full + 8 * i, 1);
+      tma::mbar_init(ring_empty + 8 * i, 1);
+    }
+    for (int i = 0; i < NB; i++) {
+      tma::mbar_init(b_full + 8 * i, 128);
+      tma::mbar_init(b_empty + 8 * i, 1);
+    }
+    for (int i = 0; i < 2; i++) {
+      tma::mbar_init(tmem_full + 8 * i, 1);
+      tma::mbar_init(tmem_empty + 8 * i, 128);
+    }
+    tma::mbar_init(drain, 1);
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 4) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tma::smem_u32(tmem_slot)),
                  "r"(tcs::kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
+  if (tid < 32)  // both W-row buffers: the padding entries stay zero
+    *reinterpret_cast<uint4*>(smem + tcs::w_off(NST, NB) + (uint32_t)tid * 16u) = make_uint4(0u, 0u, 0u, 0u);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
   const uint32_t tmem = *tmem_slot;
-
-  const uint32_t vh = A.geo.vh, nrhs = A.nrhs;
   const uint32_t p = A.parity;
-  const bool dag = A.dagger != 0;
+  const int ntiles = T.ntiles;
 
-  // TMA producer (thread 0): global hop qq of this CTA -> stage qq % NST
-  uint32_t issued = 0;
-  auto issue = [&](uint32_t qq) {
-    const int tile = (int)blockIdx.x + (int)(qq >> 3) * (int)gridDim.x;
-    if (tile >= T.ntiles) return;
-    const uint32_t st_site = (uint32_t)(tile / T.chunks), st_chunk = (uint32_t)(tile % T.chunks);
-    const int d = (int)(qq & 7u);
-    const uint32_t nbq = tc_neighbour(A, st_site, d);
-    const bool fwd = (d & 1) == 0;
-    const uint32_t lsite = fwd ? st_site : nbq, lpar = fwd ? p : 1u - p;
-    const uint32_t stage = qq % NST, bar = bar_ring + 8 * stage;
-    const uint32_t dst = smem0 + stage * tcs::kStageBytes;
-    tma::mbar_expect_tx(bar, (uint32_t)T.halves * tcs::kHalfBytes + (uint32_t)(N * N * 16));
-    for (int h = 0; h < T.halves; h++)
-      tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0, (int)nbq,
-                   bar);
-    tma::load_3d(dst + tcs::kABytes, &map_gauge, (int)(lsite & ~3u), 0, (int)(2 * (d >> 1) + lpar), bar);
-    issued = qq + 1;
-  };
-  if (tid == 0)
-    for (uint32_t qq = 0; qq + 1 < (uint32_t)NST; qq++) issue(qq);
-
-  // stage 2: this thread's two B chunks c = tid + 128 i: colour a = c & 7,
-  // input spin g = (c >> 3) & 3, output spin s = (c >> 5) & 3, part = c >> 7 = i
-  const uint32_t ca_ = (uint32_t)tid & 7u, cg = ((uint32_t)tid >> 3) & 3u, cs_ = ((uint32_t)tid >> 5) & 3u;
-  const uint32_t boff0 = cs_ * 512u + cg * 128u + ca_ * 16u;  // (n >> 3) * 512 + g * 128 + (n & 7) * 16, part 0
-  const uint32_t boff1 = boff0 + 4u * 512u;                   // part 1: n + 32
-
-  uint32_t q = 0;  // hops done by this CTA
-  bool failed = false, prod_failed = false;
-  for (int tile = blockIdx.x; tile < T.ntiles && !failed; tile += gridDim.x) {
-    const uint32_t site = (uint32_t)(tile / T.chunks), chunk = (uint32_t)(tile % T.chunks);
-
-    auto hop = [&](auto dc) -> bool {
-      constexpr int D = decltype(dc)::value;
-      constexpr int mu = D >> 1;
-      constexpr bool fwd = (D & 1) == 0;
-      constexpr bool imag = gimag(mu);
-      const uint32_t stage = q % NST, b = q & 1u;
-      const uint32_t stage_addr = smem0 + stage * tcs::kStageBytes;
-      // the hop's A block and link have landed
-      bool ok = !prod_failed && tma::mbar_wait(bar_ring + 8 * stage, (q / NST) & 1u, T.err);
-      uint32_t nb = 0;
-      float bc = 1.f;
-      if (!fwd && warp == 1) nb = tc_neighbour(A, site, D);
-      if constexpr (mu == 3) {
-        uint32_t rest, xh, y, z, t, rest2;
-        A.geo.div_hx.divmod(site, rest, xh);
-        A.geo.div_y.divmod(rest, rest2, y);
-        A.geo.div_z.divmod(rest2, t, z);
-        const uint32_t Lt = A.geo.L[3];
-        if (A.antiperiodic_t && (fwd ? t == Lt - 1 : t == 0)) bc = -1.f;
-      }
-      // stage 1 (threads 32..47): rows Re W[a][.] (j < 8) and Im W[a][.] (j >= 8),
-      // W[a][b] = U[a][b] (forward) or conj(U[b][a]) (backward), colours padded to 8
-      if (ok && warp == 1 && tid < 48) {
-        const uint32_t j = (uint32_t)tid - 32u, part = j >> 3, a = j & 7u;
-        const uint32_t sidx = (fwd ? site : nb) & 3u;
-        const uint32_t* lk = reinterpret_cast<const uint32_t*>(smem + stage * tcs::kStageBytes + tcs::kABytes);
-        uint32_t w[8];
-#pragma unroll
-        for (int bb = 0; bb < 8; bb++) {
-          uint32_t v = 0u;
-          if (bb < N && a < (uint32_t)N) v = lk[(fwd ? a * N + bb : bb * N + a) * 4u + sidx];
-          w[bb] = v;
+  if (warp < 4) {
+    // ---- B builders --------------------------------------------------------
+    // stage 2 assignment: chunks c = tid + 128 i: colour a = c & 7, input spin
+    // g = (c >> 3) & 3, output spin s = (c >> 5) & 3, part = c >> 7 = i
+    const uint32_t ca_ = (uint32_t)tid & 7u, cg = ((uint32_t)tid >> 3) & 3u, cs_ = ((uint32_t)tid >> 5) & 3u;
+    const uint32_t boff0 = cs_ * 512u + cg * 128u + ca_ * 16u;  // (n >> 3) * 512 + g * 128 + (n & 7) * 16
+    const uint32_t boff1 = boff0 + 4u * 512u;                   // part 1: n + 32
+    const bool dag = A.dagger != 0;
+    uint32_t q = 0;
+    bool stop = false;
+    for (int tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+      const uint32_t site = (uint32_t)(tile / T.chunks);
+      const uint32_t t_coord = tcs::SiteCoords(A, site).t;
+      auto hop = [&](auto dc) -> bool {
+        constexpr int D = decltype(dc)::value;
+        constexpr int mu = D >> 1;
+        constexpr bool fwd = (D & 1) == 0;
+        constexpr bool imag = gimag(mu);
+        const uint32_t st = q % NST, b = q % NB, wb = q & 1u;
+        bool ok = true;
+        // B buffer b is free once the MMAs of hop q - NB have completed
+        if (q >= NB) ok = tcs::wait(b_empty + 8 * b, ((q / NB) - 1) & 1u, T.err, abort_flag);
+        // stage 1 (threads 32 .. 32 + N*N - 1, one element of the hop's link
+        // each): the rows Re W[a][.] and Im W[a][.], W[a][b] = U[a][b]
+        // (forward) or conj(U[b][a]) (backward); the padding stays zero
+        if (ok && tid >= 32 && tid < 32 + N * N) {
+          ok = tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
+          if (ok) {
+            const uint32_t comp = (uint32_t)tid - 32u;
+            const uint32_t w =
+                reinterpret_cast<const uint32_t*>(smem + st * tcs::kStageBytes + tcs::kABytes)[comp];
+            const uint32_t a = fwd ? comp / N : comp % N, bb = fwd ? comp % N : comp / N;
+            unsigned short* wr16 = reinterpret_cast<unsigned short*>(smem + tcs::w_off(NST, NB) + wb * 256u);
+            wr16[a * 8u + bb] = (unsigned short)(w & 0xFFFFu);
+            wr16[64u + a * 8u + bb] = (unsigned short)((w >> 16) ^ (fwd ? 0u : 0x8000u));
+          }
         }
-        uint32_t o[4];
-        const uint32_t sel = part ? 0x7632u : 0x5410u;                  // high (Im) or low (Re) halves
-        const uint32_t conj = (!fwd && part) ? 0x80008000u : 0u;        // Im of conj(U)
-#pragma unroll
-        for (int i = 0; i < 4; i++) o[i] = __byte_perm(w[2 * i], w[2 * i + 1], sel) ^ conj;
-        *reinterpret_cast<uint4*>(smem + tcs::w_off(NST) + j * 16u) = make_uint4(o[0], o[1], o[2], o[3]);
-      }
-      __syncthreads();
-      // B buffer b is free once the MMAs of hop q - 2 have completed
-      if (ok && q >= 2) ok = tma::mbar_poll(bar_mma + 8 * b, ((q >> 1) - 1) & 1u, T.err);
-      if (ok) {
+        if (tcs::bar_or(1, 128, !ok)) return false;
         // stage 2: K_hop chunk for output spin s = cs_, input spin g = cg, colour a = ca_:
         // z = P[s][g] = bc (g = s) or bc * sg * (i if imag) (g = perm(s)) or 0
+        float bc = 1.f;
+        if constexpr (mu == 3) {
+          const uint32_t Lt = A.geo.L[3];
+          if (A.antiperiodic_t && (fwd ? t_coord == Lt - 1 : t_coord == 0)) bc = -1.f;
+        }
         const uint32_t perm = mu < 2 ? 3u - cs_ : (cs_ ^ 2u);
-        // gsign(mu, s) for runtime s
-        int gs;
+        int gs;  // gsign(mu, s) for runtime s
         if constexpr (mu == 0) gs = cs_ < 2 ? 1 : -1;
         else if constexpr (mu == 1) gs = (cs_ == 0 || cs_ == 3) ? -1 : 1;
         else if constexpr (mu == 2) gs = (cs_ == 0 || cs_ == 3) ? 1 : -1;
@@ -229,7 +308,7 @@ __global__ void __launch_bounds__(128)
         const bool diag = cg == cs_, off = cg == perm;
         const float sg = (diag ? 1.f : (fwd ? -1.f : 1.f) * (float)gs * (dag ? -1.f : 1.f)) * bc;
         const bool zim = off && imag;
-        const unsigned char* wr = smem + tcs::w_off(NST);
+        const unsigned char* wr = smem + tcs::w_off(NST, NB) + wb * 256u;
         unsigned char* bbuf = smem + tcs::b_off(NST) + b * tcs::kBBytes;
 #pragma unroll
         for (int part = 0; part < 2; part++) {
@@ -247,85 +326,138 @@ __global__ void __launch_bounds__(128)
           }
           *reinterpret_cast<uint4*>(bbuf + (part ? boff1 : boff0)) = v;
         }
-      }
-      tc::fence_async_smem();
-      if (__syncthreads_or(!ok)) return false;
-      if (tid == 0) {
-        tc::fence_after();
-        const uint32_t bb = smem0 + tcs::b_off(NST) + b * tcs::kBBytes;
-        // K step j: input spins 2j, 2j + 1 (two 1 KB swizzle atoms of A, two 128 B core-matrix columns of B)
-        tc::mma_bf16(tmem, tcs::a_desc(stage_addr), tcs::b_desc(bb), tcs::kIdesc, D > 0);
-        tc::mma_bf16(tmem, tcs::a_desc(stage_addr + 2048u), tcs::b_desc(bb + 256u), tcs::kIdesc, 1u);
-        tc::commit(bar_mma + 8 * b);
-        // refill the stage hop q - 1 used, once its MMAs have completed (the
-        // generic reads of its link box were ordered by this hop's barriers)
-        if (q >= 1 && !tma::mbar_poll(bar_mma + 8 * ((q - 1) & 1u), ((q - 1) >> 1) & 1u, T.err)) {
-          prod_failed = true;  // the CTA stops at the next hop's agreement
-        } else {
-          tc::fence_async_smem();
-          issue(q + NST - 1);
-        }
-      }
-      q++;
-      return true;
-    };
-    failed = !(hop(std::integral_constant<int, 0>{}) && hop(std::integral_constant<int, 1>{}) &&
+        // the tensor core reads B (and the producer refills the link copy)
+        // only after every builder's generic accesses
+        tc::fence_async_smem();
+        tma::mbar_arrive(b_full + 8 * b);
+        q++;
+        return true;
+      };
+      stop = !(hop(std::integral_constant<int, 0>{}) && hop(std::integral_constant<int, 1>{}) &&
                hop(std::integral_constant<int, 2>{}) && hop(std::integral_constant<int, 3>{}) &&
                hop(std::integral_constant<int, 4>{}) && hop(std::integral_constant<int, 5>{}) &&
                hop(std::integral_constant<int, 6>{}) && hop(std::integral_constant<int, 7>{}));
-    if (failed) break;
-
-    // the commit of the last hop covers all MMAs of this tile
-    const uint32_t ql = q - 1;
-    const bool ok = tma::mbar_poll(bar_mma + 8 * (ql & 1u), (ql >> 1) & 1u, T.err);
-    if (__syncthreads_or(!ok)) {
-      failed = true;
-      break;
     }
-    tc::fence_after();
-
-    // epilogue, one output spin at a time: lane m = 2 r + ri holds part ri of
-    // RHS r; Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K
-    const uint32_t r = (uint32_t)tid >> 1, ri = (uint32_t)tid & 1u;
-    const uint32_t rhs = chunk * (uint32_t)T.rt + r;
-    const bool live = r < (uint32_t)T.rt && (!A.mask || A.mask[rhs] != 0);
-    const float ca = live ? (A.a_rhs_f ? A.a_rhs_f[rhs] : A.af) : 0.f;
+  } else if (warp == 4) {
+    // ---- MMA issuer ----------------------------------------------------------
+    if (lane == 0) {
+      uint32_t q = 0;
+      bool ok = true;
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+        const uint32_t acc = (uint32_t)it & 1u;
+        // the epilogue has read this accumulator's previous tile
+        if (it >= 2) ok = tcs::wait(tmem_empty + 8 * acc, (((uint32_t)it >> 1) - 1) & 1u, T.err, abort_flag);
+        tc::fence_after();
+        for (int h = 0; h < 8 && ok; h++, q++) {
+          const uint32_t st = q % NST, b = q % NB;
+          ok = tcs::wait(b_full + 8 * b, (q / NB) & 1u, T.err, abort_flag) &&
+               tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
+          if (!ok) break;
+          tc::fence_after();
+          const uint32_t sa = smem0 + st * tcs::kStageBytes;
+          const uint32_t sb = smem0 + tcs::b_off(NST) + b * tcs::kBBytes;
+          const uint32_t d = tmem + acc * 64u;
+          // K step j: input spins 2j, 2j + 1 (two 1 KB swizzle atoms of A, two 128 B core-matrix columns of B)
+          tc::mma_bf16(d, tcs::a_desc(sa), tcs::b_desc(sb), tcs::kIdesc, h > 0);
+          tc::mma_bf16(d, tcs::a_desc(sa + 2048u), tcs::b_desc(sb + 256u), tcs::kIdesc, 1u);
+          tc::commit(b_empty + 8 * b);
+          tc::commit(ring_empty + 8 * st);
+        }
+        if (ok) tc::commit(tmem_full + 8 * acc);
+      }
+      // every MMA issued has completed before the tensor memory is released (bounded)
+      tc::commit(drain);
+      tma::mbar_wait(drain, 0, T.err);
+    }
+  } else if (warp == 5) {
+    // ---- TMA producer --------------------------------------------------------
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_in)) : "memory");
+      constexpr uint32_t kLink = (uint32_t)((4 * N * N + 15) / 16 * 16);  // layout.h tc_link_bytes
+      const unsigned char* gtc = static_cast<const unsigned char*>(A.gauge_tc);
+      const uint32_t vh = A.geo.vh;
+      const uint32_t tx = (uint32_t)T.halves * tcs::kHalfBytes + kLink;
+      const uint64_t keep = tcs::evict_last_policy();
+      uint32_t qq = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const uint32_t st_site = (uint32_t)(tile / T.chunks), st_chunk = (uint32_t)(tile % T.chunks);
+        const tcs::SiteCoords sc(A, st_site);
+#pragma unroll
+        for (int d = 0; d < 8; d++, qq++) {
+          const uint32_t st = qq % NST;
+          // stage st is free once the MMAs of hop qq - NST have completed
+          if (qq >= (uint32_t)NST && !tcs::wait(ring_empty + 8 * st, ((qq / NST) - 1) & 1u, T.err, abort_flag)) {
+            ok = false;
+            break;
+          }
+          const uint32_t nbq = sc.nb(A, d);
+          const uint32_t lsite = (d & 1) ? nbq : st_site, lpar = (d & 1) ? 1u - p : p;
+          const uint32_t bar = ring_full + 8 * st, dst = smem0 + st * tcs::kStageBytes;
+          tma::mbar_expect_tx(bar, tx);
+          for (int h = 0; h < T.halves; h++)
+            tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0,
+                         (int)nbq, bar, keep);
+          tcs::bulk_load(dst + tcs::kABytes, gtc + ((uint64_t)(2 * (d >> 1) + lpar) * vh + lsite) * kLink, kLink, bar);
+        }
+      }
+      // copies still in flight land before the CTA's shared memory is released (bounded):
+      // the last hop issued into each stage
+      for (uint32_t k = 0; k < (uint32_t)NST && k < qq; k++) {
+        const uint32_t last = qq - 1 - k;
+        tma::mbar_wait(ring_full + 8 * (last % NST), (last / NST) & 1u, T.err);
+      }
+    }
+  } else {
+    // ---- epilogue (warps 6-9: lane quarter warp % 4) ---------------------------
+    const uint32_t lq = (uint32_t)warp & 3u;
+    const uint32_t m = lq * 32u + (uint32_t)lane;
+    const uint32_t r = m >> 1, ri = m & 1u;
+    const uint32_t vh = A.geo.vh, nrhs = A.nrhs, cs = vh * nrhs;
     const __nv_bfloat16* __restrict__ xin = static_cast<const __nv_bfloat16*>(A.x);
     __nv_bfloat16* __restrict__ out = static_cast<__nv_bfloat16*>(A.out);
-    const uint32_t cs = vh * nrhs;
-    const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+      const uint32_t site = (uint32_t)(tile / T.chunks), chunk = (uint32_t)(tile % T.chunks);
+      const uint32_t rhs = chunk * (uint32_t)T.rt + r;
+      const bool live = r < (uint32_t)T.rt && (!A.mask || A.mask[rhs] != 0);
+      const float ca = live ? (A.a_rhs_f ? A.a_rhs_f[rhs] : A.af) : 0.f;
+      const uint32_t acc = (uint32_t)it & 1u;
+      if (!tcs::wait(tmem_full + 8 * acc, ((uint32_t)it >> 1) & 1u, T.err, abort_flag)) break;
+      tc::fence_after();
+      const uint32_t lane_addr = tmem + ((lq * 32u) << 16) + acc * 64u;
+      // Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
-      uint32_t re_k[8], im_k[8];
-      tcs::ld8(lane_addr + 8u * s, re_k);
-      tcs::ld8(lane_addr + 32u + 8u * s, im_k);
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      for (int s = 0; s < 4; s++) {
+        uint32_t re_k[8], im_k[8];
+        tcs::ld8(lane_addr + 8u * s, re_k);
+        tcs::ld8(lane_addr + 32u + 8u * s, im_k);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (s == 3) {
+          // the accumulator is free for the tile after next once all its columns are read
+          tc::fence_before();
+          tma::mbar_arrive(tmem_empty + 8 * acc);
+        }
 #pragma unroll
-      for (int a = 0; a < N; a++) {
-        const float other = __shfl_xor_sync(0xffffffffu, __uint_as_float(im_k[a]), 1);
-        const float own = __uint_as_float(re_k[a]);
-        float val = ca * (ri ? own + other : own - other);
-        if (live) {
-          const uint32_t idx = 2u * ((uint32_t)(s * N + a) * cs + site * nrhs + rhs) + ri;
-          if (xin) val = fmaf(A.bf, __bfloat162float(xin[idx]), val);
-          out[idx] = __float2bfloat16_rn(val);
+        for (int a = 0; a < N; a++) {
+          const float other = __shfl_xor_sync(0xffffffffu, __uint_as_float(im_k[a]), 1);
+          const float own = __uint_as_float(re_k[a]);
+          float val = ca * (ri ? own + other : own - other);
+          if (live) {
+            const uint32_t idx = 2u * ((uint32_t)(s * N + a) * cs + site * nrhs + rhs) + ri;
+            if (xin) val = fmaf(A.bf, __bfloat162float(xin[idx]), val);
+            // streaming store: the output is not re-read by this launch
+            __stcs(reinterpret_cast<unsigned short*>(out) + idx, __bfloat16_as_ushort(__float2bfloat16_rn(val)));
+          }
         }
       }
     }
-    tc::fence_before();
   }
 
-  if (failed && tid == 0 && q > 0) {
-    // let the MMAs in flight finish before the tensor memory is released (bounded)
-    const uint32_t ql = q - 1;
-    tma::mbar_poll(bar_mma + 8 * (ql & 1u), (ql >> 1) & 1u, T.err);
-  }
-  // copies still in flight land before the CTA's shared memory is released (bounded)
-  if (failed && tid == 0)
-    for (uint32_t qq = q; qq < issued; qq++) tma::mbar_poll(bar_ring + 8 * (qq % NST), (qq / NST) & 1u, T.err);
   tc::fence_before();
   __syncthreads();
-  if (warp == 0)
+  if (warp == 4)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcs::kTmemCols) : "memory");
 }
 

@@ -404,6 +404,34 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 
+namespace {
+// one thread per 4-byte word of the destination (padding words written as 0)
+__global__ void gauge_site_major_kernel(const double2* __restrict__ src, uint32_t* __restrict__ dst, int64_t vh,
+                                        int nn, int words) {
+  const int64_t n = 8 * vh * words;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int64_t w = i % words, ls = i / words, site = ls % vh, blk = ls / vh;
+    uint32_t v = 0u;
+    if (w < nn) {
+      const double2 u = src[(blk * nn + w) * vh + site];
+      const __nv_bfloat162 b = __floats2bfloat162_rn((float)u.x, (float)u.y);
+      v = *reinterpret_cast<const uint32_t*>(&b);
+    }
+    dst[i] = v;
+  }
+}
+}  // namespace
+
+void gauge_site_major_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st) {
+  const int words = tc_link_bytes(N) / 4;
+  const int block = 256;
+  const int grid = (int)std::min<int64_t>((8 * vh * words + block - 1) / block, 152 * 32);
+  gauge_site_major_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), static_cast<uint32_t*>(dst),
+                                                  vh, N * N, words);
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+
 double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st) {
   QCU_CHECK_CUDA(cudaMemsetAsync(scratch, 0, sizeof(unsigned), st));
   const int block = 256;

@@ -43,6 +43,11 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
 // max over the links of |row 2 - conj(row 0 x row 1)| (0 for exact SU(3));
 // scratch: one device unsigned
 double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st);
+// BF16 links in site-major order for the tensor-core dslash: [8 (mu, parity)]
+// [Vh][N*N] complex BF16, each link padded to tc_link_bytes(N) (a multiple of
+// 16 bytes, so one bulk copy moves a link); from the FP64 master [8][N*N][Vh]
+inline int tc_link_bytes(int N) { return (4 * N * N + 15) / 16 * 16; }
+void gauge_site_major_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st);
 // plain complex-double transpose [rows][cols] -> [cols][rows]
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st);
 

@@ -267,6 +267,7 @@ void Session::load_gauge(const void* caller_gauge, int lex) {
   void* d = gauge_[PREC_DOUBLE].ensure(bytes);
   pack_gauge(PREC_DOUBLE, N, caller_gauge, lex, d, geo, stream());
   for (int p = 0; p < 5; p++) gauge_valid_[p] = gauge12_valid_[p] = false;
+  gauge_tc_valid_ = false;
   gauge_valid_[PREC_DOUBLE] = true;
   su3_dev_ = -1.0;
   gauge_loaded_ = true;
@@ -302,6 +303,16 @@ const void* Session::gauge12(int prec) {
     gauge12_valid_[prec] = true;
   }
   return gauge12_[prec].get();
+}
+
+const void* Session::gauge_tc() {
+  QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
+  if (!gauge_tc_valid_) {
+    void* d = gauge_tc_.ensure((size_t)8 * geo.vh * tc_link_bytes(N));
+    gauge_site_major_bf16(N, gauge_[PREC_DOUBLE].get(), d, geo.vh, stream());
+    gauge_tc_valid_ = true;
+  }
+  return gauge_tc_.get();
 }
 
 void Session::load_clover(const void* caller_clover) {
@@ -378,6 +389,8 @@ void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagg
   DslashArgs A;
   A.gauge = gauge(in.prec);
   A.gauge12 = gauge12(in.prec);
+  // BF16 RHS counts the spinor-operand tensor-core kernel takes
+  if (in.prec == PREC_BF16 && in.nrhs % 4 == 0) A.gauge_tc = gauge_tc();
   A.in = in.data;
   A.in_norm = in.norm;
   A.out = out.data;

@@ -151,6 +151,9 @@ class Session {
   // `prec`), or nullptr when the loaded field is not SU(3) to that precision's
   // rounding (then the third rows are not reconstructible)
   const void* gauge12(int prec);
+  // the links in BF16, site-major (layout.h gauge_site_major_bf16), for the
+  // spinor-operand tensor-core dslash; built on first use
+  const void* gauge_tc();
 
   // ---- clover term (clover.h) ---------------------------------------------
   // caller field [2][Vh][2][2N][2N] complex double, Hermitian blocks; packed
@@ -185,6 +188,8 @@ class Session {
   bool gauge_valid_[5] = {false, false, false, false, false};
   DeviceBuffer gauge12_[5];
   bool gauge12_valid_[5] = {false, false, false, false, false};
+  DeviceBuffer gauge_tc_;
+  bool gauge_tc_valid_ = false;
   double su3_dev_ = -1.0;  // max |row 2 - conj(row 0 x row 1)|, < 0: not measured
   DeviceBuffer su3_scratch_;
   bool clover_loaded_ = false;
