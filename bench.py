@@ -560,24 +560,29 @@ def colors_bench(torch, Q, peak, fma):
         Q.initGridSize(L, n)
         Q.set_antiperiodic_t(True)
         Q.loadQcuGauge(g_dev.data_ptr())
-        prm = Q.solver_params(kappa=0.11, tol=1e-8, inner_precision=Q.QCU_SINGLE_PRECISION,
-                              solver=Q.QCU_SOLVER_BICGSTAB, max_iter=5000)
-        for phase in ("cold", "warm"):
-            x.zero_()
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            Q.invert([x[r].data_ptr() for r in range(nr)], [b[r].data_ptr() for r in range(nr)], prm,
-                     raise_on_error=False)
-            torch.cuda.synchronize()
-            sec = time.perf_counter() - t0
-        solves.append({"N": n, "nrhs": nr, "seconds": round(sec, 4), "iterations": prm.iterations,
-                       "max_true_residual": max(prm.true_residual[r] for r in range(nr)),
-                       "all_converged": all(prm.converged[r] for r in range(nr))})
+        # FP32 inner (CUDA-core dslash) and BF16 inner (the autotuner's dslash: tensor cores where they win)
+        for inner, iname in ((Q.QCU_SINGLE_PRECISION, "fp32"), (Q.QCU_BF16_PRECISION, "bf16")):
+            prm = Q.solver_params(kappa=0.11, tol=1e-8, inner_precision=inner,
+                                  solver=Q.QCU_SOLVER_BICGSTAB, max_iter=5000)
+            for phase in ("cold", "warm"):
+                x.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                Q.invert([x[r].data_ptr() for r in range(nr)], [b[r].data_ptr() for r in range(nr)], prm,
+                         raise_on_error=False)
+                torch.cuda.synchronize()
+                sec = time.perf_counter() - t0
+            _, _, _, _, st_bf, _ = Q.tune_dslash(nr, inner)
+            solves.append({"N": n, "nrhs": nr, "inner": iname, "seconds": round(sec, 4),
+                           "iterations": prm.iterations, "reliable_updates": prm.reliable_updates,
+                           "inner_dslash": ("tensor_core_variant_%d" % -st_bf) if st_bf < 0 else "cuda_core",
+                           "max_true_residual": max(prm.true_residual[r] for r in range(nr)),
+                           "all_converged": all(prm.converged[r] for r in range(nr))})
         del g_dev, psi, b, x
         torch.cuda.empty_cache()
     return {"workload": "16^3x32 SU(N) dslash: FP32 storage on CUDA cores; BF16 storage on CUDA cores (FP32 "
                         "arithmetic) and on the tensor cores (tcgen05, BF16 operands, FP32 accumulation); "
-                        "BiCGStab kappa 0.11, FP32 inner, 16 RHS (one 1e-4 smaller, one zero) to 1e-8",
+                        "BiCGStab kappa 0.11, FP32 and BF16 inner, 16 RHS (one 1e-4 smaller, one zero) to 1e-8",
             "dslash": rows, "bicgstab": solves}
 
 

@@ -143,8 +143,8 @@ int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_
  * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
  * 6 = 104), whether the packed FP32x2 arithmetic variant was chosen, and the
  * ring depth of the TMA-staged kernel (0: the register kernel was chosen;
- * -1: the tensor-core kernel with direct loads, -2 / -3: with a TMA ring of
- * that depth), and whether the kernel reads two-row SU(3) links (recon = 1). */
+ * -v: tensor-core variant v, see qcuDslashKernels), and whether the kernel
+ * reads two-row SU(3) links (recon = 1). */
 int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed, int *stages,
                   int *recon);
 
@@ -158,12 +158,14 @@ int qcuMeasureFmaRate(int precision, double *tflops);
  * (RHS per thread, register-cap variant, packed, stages, recon) are
  * available; the first max_shapes are written to shapes[5 * i .. 5 * i + 4].
  * stages > 0 is the TMA-staged kernel with that many ring buffers, stages < 0
- * the tensor-core (tcgen05) kernel (-1 direct loads, -2 / -3 a TMA ring of
- * that depth); recon = 1 reads SU(3) links as two rows
- * and reconstructs the third (used only when the loaded gauge is SU(3) to the
- * precision's rounding).  Any shape can be pinned with
- * QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon"
- * (tensor = 1, 2, 3 for the tensor-core variants). */
+ * a tensor-core (tcgen05) kernel, BF16 only: -1 projected half-spinor
+ * operands with direct loads, -2 / -3 the same with a TMA ring of that depth,
+ * -4 / -5 / -6 the neighbour spinor block as the MMA operand (warp-specialised,
+ * TMA and B rings of different depths; nrhs a multiple of 4); recon = 1 reads
+ * SU(3) links as two rows and reconstructs the third (used only when the
+ * loaded gauge is SU(3) to the precision's rounding).  Any shape can be
+ * pinned with QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon"
+ * (tensor = 1..6 for the tensor-core variants). */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 
 typedef struct QcuSolverParam_s {

@@ -308,8 +308,9 @@ def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:
 
 def tune_dslash(nrhs: int, precision: int):
     """(R, block, reg_cap, packed, stages, recon) of the tuned kernel; stages
-    > 0: the TMA-staged kernel, -1: the tensor-core kernel; recon: two-row
-    SU(3) links."""
+    > 0: the TMA-staged kernel, -v: tensor-core variant v (1-3 projected
+    half-spinor operands, 4-6 the spinor block as the MMA operand); recon:
+    two-row SU(3) links."""
     R, B, M, K, T, C = (ctypes.c_int() for _ in range(6))
     _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M),
                                   ctypes.byref(K), ctypes.byref(T), ctypes.byref(C)))
@@ -318,8 +319,8 @@ def tune_dslash(nrhs: int, precision: int):
 
 def dslash_kernels(precision: int, n_colors: int = 3):
     """Compiled dslash kernel shapes [(R, reg_cap, packed, stages, recon), ...];
-    stages > 0: the TMA-staged kernel, -1: the tensor-core kernel; recon: two-row
-    SU(3) links."""
+    stages > 0: the TMA-staged kernel, -v: tensor-core variant v (1-6); recon:
+    two-row SU(3) links."""
     arr = (ctypes.c_int * (5 * 64))()
     cnt = ctypes.c_int()
     _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
