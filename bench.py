@@ -381,12 +381,19 @@ def run_gpu(args):
         run(e2e_steps, f0, f1)
         torch.cuda.synchronize()
         ems = max_over_ranks(dist, f0.elapsed_time(f1) / e2e_steps)
+        # the downloaded results equal one untimed call of the same ABI on device buffers
+        for r in range(nrhs):
+            Q.pushBackFermions(dev_out[0][r].data_ptr(), dev_in[1][r].data_ptr())
+        Q.startDslash(0, 0)
+        torch.cuda.synchronize()
+        e2e_same = all(torch.equal(host_out[r], dev_out[0][r].cpu()) for r in range(nrhs))
         bytes_io = nrhs * vh * 4 * n * 16
         e2e = {"value": job_throughput(units, world, ems), "unit": "site*RHS/s", "h2d_bytes_per_step": bytes_io,
                "d2h_bytes_per_step": bytes_io, "ms_per_step": round(ems, 3), "steps": e2e_steps,
                "path": "pinned host -> upload stream -> pushBackFermions x12 + startDslash -> download stream -> "
                        "pinned host (FP64 caller layout); device buffers double buffered so step k+1's upload "
-                       "and step k-1's download overlap step k"}
+                       "and step k-1's download overlap step k",
+               "results_equal_device_path": e2e_same}
         Q.set_stream(None)
         del host_in, host_out, dev_in, dev_out
 
