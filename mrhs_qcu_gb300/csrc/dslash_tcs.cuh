@@ -28,17 +28,16 @@
 //
 // Persistent, warp-specialized CTA of 320 threads; the roles hand work to
 // each other through mbarriers only:
-//   warps 0-3  B builders: per hop, the link rows W (threads 32 .. 32+N*N-1,
-//              one element each of the hop's link, copied with the A block)
-//              and the 4 KB B operand into a ring of NB buffers; one named
-//              barrier per hop between the two steps
+//   warps 0-3  B builders: per hop, the 4 KB B operand into a ring of NB
+//              buffers, each thread two 16-byte chunks: signed copies of one
+//              link row that arrived with the A block
 //   warp 4     MMA issuer (one thread): two MMAs per hop into one of two
 //              tensor-memory accumulators; commits free the B buffer and the
 //              TMA stage, and hand a finished tile to the epilogue
 //   warp 5     TMA producer (one thread): per hop, the neighbour's A block
-//              (one or two boxes of 32 RHS) and the link (one bulk copy from
-//              the site-major BF16 links, layout.h gauge_site_major_bf16)
-//              into a ring of NST stages, as far ahead as the ring allows
+//              (one or two boxes of 32 RHS) and the link in row form (one
+//              256-byte bulk copy, layout.h gauge_tc_rows_bf16) into a ring
+//              of NST stages, as far ahead as the ring allows
 //   warps 6-9  epilogue: tensor memory -> Re/Im combination -> global, one
 //              tile behind the MMAs (double-buffered accumulator)
 // Every wait is bounded (about 1 s); a timeout sets *err and a shared abort
@@ -66,16 +65,15 @@ namespace tcs {
 
 constexpr uint32_t kHalfBytes = 4096;               // 4 spins x 8 colours x 128 B
 constexpr uint32_t kABytes = 2 * kHalfBytes;        // M = 128 rows
-constexpr uint32_t kLinkBytes = 1024;               // one site-major link (<= 256 B), 1 KB keeps stages aligned
+constexpr uint32_t kLinkBytes = 1024;               // one link in row form (256 B), 1 KB keeps stages aligned
 constexpr uint32_t kStageBytes = kABytes + kLinkBytes;
 constexpr uint32_t kBBytes = 4096;                  // 64 (n) x 32 (k) BF16, K-major
 constexpr uint32_t kTmemCols = 128;  // two accumulators of 64 columns
 
 // offsets from the 1024-byte aligned base of dynamic shared memory: TMA
-// stages, B buffers, two W-row buffers, barriers
+// stages, B buffers, barriers
 __host__ __device__ constexpr uint32_t b_off(int nst) { return (uint32_t)nst * kStageBytes; }
-__host__ __device__ constexpr uint32_t w_off(int nst, int nb) { return b_off(nst) + (uint32_t)nb * kBBytes; }
-__host__ __device__ constexpr uint32_t bar_off(int nst, int nb) { return w_off(nst, nb) + 512; }
+__host__ __device__ constexpr uint32_t bar_off(int nst, int nb) { return b_off(nst) + (uint32_t)nb * kBBytes; }
 // barriers: ring_full[nst], ring_empty[nst], b_full[nb], b_empty[nb],
 // tmem_full[2], tmem_empty[2], drain; then the tensor-memory slot and the abort flag
 __host__ __device__ constexpr uint32_t slot_off(int nst, int nb) { return bar_off(nst, nb) + 8u * (2 * nst + 2 * nb + 5); }
@@ -183,17 +181,6 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, vo
   }
 }
 
-// named barrier `id` over `count` threads with an OR reduction of `pred`
-__device__ __forceinline__ bool bar_or(int id, int count, bool pred) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}"
-      : "=r"(r)
-      : "r"((uint32_t)pred), "r"(id), "r"(count)
-      : "memory");
-  return r != 0;
-}
-
 }  // namespace tcs
 
 // map_in: the input field as [site][spin 4][colour N][RHS] of 4-byte complex
@@ -245,8 +232,6 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
-  if (tid < 32)  // both W-row buffers: the padding entries stay zero
-    *reinterpret_cast<uint4*>(smem + tcs::w_off(NST, NB) + (uint32_t)tid * 16u) = make_uint4(0u, 0u, 0u, 0u);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -272,26 +257,13 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
         constexpr int mu = D >> 1;
         constexpr bool fwd = (D & 1) == 0;
         constexpr bool imag = gimag(mu);
-        const uint32_t st = q % NST, b = q % NB, wb = q & 1u;
+        const uint32_t st = q % NST, b = q % NB;
+        // B buffer b is free once the MMAs of hop q - NB have completed; the
+        // hop's link rows arrive with its A block
         bool ok = true;
-        // B buffer b is free once the MMAs of hop q - NB have completed
         if (q >= NB) ok = tcs::wait(b_empty + 8 * b, ((q / NB) - 1) & 1u, T.err, abort_flag);
-        // stage 1 (threads 32 .. 32 + N*N - 1, one element of the hop's link
-        // each): the rows Re W[a][.] and Im W[a][.], W[a][b] = U[a][b]
-        // (forward) or conj(U[b][a]) (backward); the padding stays zero
-        if (ok && tid >= 32 && tid < 32 + N * N) {
-          ok = tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
-          if (ok) {
-            const uint32_t comp = (uint32_t)tid - 32u;
-            const uint32_t w =
-                reinterpret_cast<const uint32_t*>(smem + st * tcs::kStageBytes + tcs::kABytes)[comp];
-            const uint32_t a = fwd ? comp / N : comp % N, bb = fwd ? comp % N : comp / N;
-            unsigned short* wr16 = reinterpret_cast<unsigned short*>(smem + tcs::w_off(NST, NB) + wb * 256u);
-            wr16[a * 8u + bb] = (unsigned short)(w & 0xFFFFu);
-            wr16[64u + a * 8u + bb] = (unsigned short)((w >> 16) ^ (fwd ? 0u : 0x8000u));
-          }
-        }
-        if (tcs::bar_or(1, 128, !ok)) return false;
+        if (ok) ok = tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
+        if (!ok) return false;
         // stage 2: K_hop chunk for output spin s = cs_, input spin g = cg, colour a = ca_:
         // z = P[s][g] = bc (g = s) or bc * sg * (i if imag) (g = perm(s)) or 0
         float bc = 1.f;
@@ -308,7 +280,9 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
         const bool diag = cg == cs_, off = cg == perm;
         const float sg = (diag ? 1.f : (fwd ? -1.f : 1.f) * (float)gs * (dag ? -1.f : 1.f)) * bc;
         const bool zim = off && imag;
-        const unsigned char* wr = smem + tcs::w_off(NST, NB) + wb * 256u;
+        // link rows in the stage: row (part, a) of W = U (forward) or of U^T
+        // (backward, whose conjugation flips the sign of the Im part)
+        const unsigned char* wr = smem + st * tcs::kStageBytes + tcs::kABytes;
         unsigned char* bbuf = smem + tcs::b_off(NST) + b * tcs::kBBytes;
 #pragma unroll
         for (int part = 0; part < 2; part++) {
@@ -316,7 +290,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           if (diag || off) {
             const uint32_t src = (uint32_t)part ^ (zim ? 1u : 0u);
             // z real: sign sg on both parts; z = sg i: Re part -sg Im W, Im part +sg Re W
-            const bool neg = zim ? (part == 0 ? sg > 0.f : sg < 0.f) : sg < 0.f;
+            const bool neg = (zim ? (part == 0 ? sg > 0.f : sg < 0.f) : sg < 0.f) != (!fwd && src == 1u);
             const uint32_t m = neg ? 0x80008000u : 0u;
             v = *reinterpret_cast<const uint4*>(wr + (src * 8u + ca_) * 16u);
             v.x ^= m;
@@ -326,8 +300,8 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           }
           *reinterpret_cast<uint4*>(bbuf + (part ? boff1 : boff0)) = v;
         }
-        // the tensor core reads B (and the producer refills the link copy)
-        // only after every builder's generic accesses
+        // the tensor core reads B, and the producer refills the stage, only
+        // after every builder's generic accesses
         tc::fence_async_smem();
         tma::mbar_arrive(b_full + 8 * b);
         q++;
@@ -374,7 +348,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     // ---- TMA producer --------------------------------------------------------
     if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_in)) : "memory");
-      constexpr uint32_t kLink = (uint32_t)((4 * N * N + 15) / 16 * 16);  // layout.h tc_link_bytes
+      constexpr uint32_t kLink = 256;  // layout.h kTcLinkBytes
       const unsigned char* gtc = static_cast<const unsigned char*>(A.gauge_tc);
       const uint32_t vh = A.geo.vh;
       const uint32_t tx = (uint32_t)T.halves * tcs::kHalfBytes + kLink;
@@ -399,7 +373,9 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           for (int h = 0; h < T.halves; h++)
             tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0,
                          (int)nbq, bar, keep);
-          tcs::bulk_load(dst + tcs::kABytes, gtc + ((uint64_t)(2 * (d >> 1) + lpar) * vh + lsite) * kLink, kLink, bar);
+          // form 0 (rows of U) for forward hops, form 1 (rows of U^T) for backward ones
+          tcs::bulk_load(dst + tcs::kABytes,
+                         gtc + ((uint64_t)((d & 1) * 8 + 2 * (d >> 1) + lpar) * vh + lsite) * kLink, kLink, bar);
         }
       }
       // copies still in flight land before the CTA's shared memory is released (bounded):

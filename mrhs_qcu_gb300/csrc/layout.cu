@@ -405,30 +405,37 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
 }
 
 namespace {
-// one thread per 4-byte word of the destination (padding words written as 0)
-__global__ void gauge_site_major_kernel(const double2* __restrict__ src, uint32_t* __restrict__ dst, int64_t vh,
-                                        int nn, int words) {
-  const int64_t n = 8 * vh * words;
+// one thread per 4-byte word (two BF16 of adjacent columns) of the destination
+__global__ void gauge_tc_rows_kernel(const double2* __restrict__ src, uint32_t* __restrict__ dst, int64_t vh,
+                                     int N) {
+  const int64_t n = 2 * 8 * vh * 64;  // 64 words per link and form
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int64_t w = i % words, ls = i / words, site = ls % vh, blk = ls / vh;
-    uint32_t v = 0u;
-    if (w < nn) {
-      const double2 u = src[(blk * nn + w) * vh + site];
-      const __nv_bfloat162 b = __floats2bfloat162_rn((float)u.x, (float)u.y);
-      v = *reinterpret_cast<const uint32_t*>(&b);
+    const int w = (int)(i & 63);
+    const int64_t link = i >> 6;  // (form * 8 + blk) * vh + site
+    const int64_t site = link % vh, fb = link / vh, blk = fb % 8, form = fb / 8;
+    const int part = w >> 5, row = (w >> 2) & 7, c0 = 2 * (w & 3);
+    float v[2] = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int col = c0 + k;
+      if (row < N && col < N) {
+        const int comp = form == 0 ? row * N + col : col * N + row;  // U[row][col] or U[col][row]
+        const double2 u = src[(blk * N * N + comp) * vh + site];
+        v[k] = (float)(part ? u.y : u.x);
+      }
     }
-    dst[i] = v;
+    const __nv_bfloat162 b = __floats2bfloat162_rn(v[0], v[1]);
+    dst[i] = *reinterpret_cast<const uint32_t*>(&b);
   }
 }
 }  // namespace
 
-void gauge_site_major_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st) {
-  const int words = tc_link_bytes(N) / 4;
+void gauge_tc_rows_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st) {
   const int block = 256;
-  const int grid = (int)std::min<int64_t>((8 * vh * words + block - 1) / block, 152 * 32);
-  gauge_site_major_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), static_cast<uint32_t*>(dst),
-                                                  vh, N * N, words);
+  const int grid = (int)std::min<int64_t>((2 * 8 * vh * 64 + block - 1) / block, 152 * 32);
+  gauge_tc_rows_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), static_cast<uint32_t*>(dst), vh,
+                                               N);
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 

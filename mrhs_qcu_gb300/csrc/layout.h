@@ -43,11 +43,16 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
 // max over the links of |row 2 - conj(row 0 x row 1)| (0 for exact SU(3));
 // scratch: one device unsigned
 double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st);
-// BF16 links in site-major order for the tensor-core dslash: [8 (mu, parity)]
-// [Vh][N*N] complex BF16, each link padded to tc_link_bytes(N) (a multiple of
-// 16 bytes, so one bulk copy moves a link); from the FP64 master [8][N*N][Vh]
-inline int tc_link_bytes(int N) { return (4 * N * N + 15) / 16 * 16; }
-void gauge_site_major_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st);
+// BF16 links for the spinor-operand tensor-core dslash, site-major and
+// already split into the rows its link operand is built from:
+// [form 2][8 (mu, parity)][Vh][part 2][row 8][col 8] BF16, 256 bytes per link
+// and form (one bulk copy), rows and columns >= N zero.  Form 0 holds the
+// rows of U (part 0 Re, part 1 Im), for forward hops; form 1 the rows of U^T
+// (the columns of U), for backward hops, which use conj(U^T).  Built from the
+// FP64 master [8][N*N][Vh].
+constexpr int kTcLinkBytes = 256;
+inline size_t tc_links_bytes(int64_t vh) { return (size_t)2 * 8 * vh * kTcLinkBytes; }
+void gauge_tc_rows_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st);
 // plain complex-double transpose [rows][cols] -> [cols][rows]
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st);
 

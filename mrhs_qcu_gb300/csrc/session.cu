@@ -308,8 +308,8 @@ const void* Session::gauge12(int prec) {
 const void* Session::gauge_tc() {
   QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
   if (!gauge_tc_valid_) {
-    void* d = gauge_tc_.ensure((size_t)8 * geo.vh * tc_link_bytes(N));
-    gauge_site_major_bf16(N, gauge_[PREC_DOUBLE].get(), d, geo.vh, stream());
+    void* d = gauge_tc_.ensure(tc_links_bytes(geo.vh));
+    gauge_tc_rows_bf16(N, gauge_[PREC_DOUBLE].get(), d, geo.vh, stream());
     gauge_tc_valid_ = true;
   }
   return gauge_tc_.get();
