@@ -535,12 +535,10 @@ def colors_bench(torch, Q, peak, fma):
         # FP32: the autotuned CUDA-core kernel; BF16: CUDA cores (register kernel, R = 2) and the
         # tensor-core (tcgen05) kernel, each pinned
         for p, pname, kernel, pin in ((1, "fp32", "cuda_core", None), (4, "bf16", "cuda_core", "2,64,1,0"),
-                                      (4, "bf16", "tensor_core", "1,0,0,0,0,0,1"),
-                                      (4, "bf16", "tensor_core_tma2", "1,0,0,0,0,0,2"),
-                                      (4, "bf16", "tensor_core_tma3", "1,0,0,0,0,0,3"),
-                                      (4, "bf16", "tensor_core_spinor2", "1,0,0,0,0,0,4"),
-                                      (4, "bf16", "tensor_core_spinor3", "1,0,0,0,0,0,5"),
-                                      (4, "bf16", "tensor_core_spinor4", "1,0,0,0,0,0,6")):
+                                      (4, "bf16", "tensor_core_projected", "1,0,0,0,0,0,1"),
+                                      (4, "bf16", "tensor_core_projected_tma", "1,0,0,0,0,0,2"),
+                                      (4, "bf16", "tensor_core_spinor", "1,0,0,0,0,0,4"),
+                                      (4, "bf16", "tensor_core_spinor_deep", "1,0,0,0,0,0,5")):
             for nr in (16, 32, 64):
                 if pin:
                     os.environ["QCU_DSLASH_CONFIG"] = pin
