@@ -185,7 +185,7 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, vo
 
 // map_in: the input field as [site][spin 4][colour N][RHS] of 4-byte complex
 // BF16, box (32 RHS, 8 colours, 4 spins, 1 site), 128-byte swizzle.  The
-// links come from A.gauge_tc (site-major BF16, one bulk copy per hop).
+// links come from A.gauge_tc (BF16 row form, one 256-byte bulk copy per hop).
 template <int N, int NST, int NB>
 __global__ void __launch_bounds__(tcs::kThreads, 4)
     wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
