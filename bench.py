@@ -52,6 +52,16 @@ FLOPS_PER_SITE_RHS = lambda n: 128 * n * n + 56 * n  # noqa: E731
 METRIC = "dslash site\u00b7RHS/s & % HBM roofline; mixed vs FP64 solve time @1e-10; p99"
 
 
+def workload_config(L, n, nrhs, world, precision):
+    """The workload both arms measure; `precision` is the arm's storage
+    (ours) or arithmetic (the reference's FP64 CPU path) precision."""
+    return {"workload": "MRHS even-odd Wilson dslash D_eo, SU(%d), %s, nrhs=%d, antiperiodic t"
+                        % (n, "x".join(map(str, L)), nrhs),
+            "lattice": list(L), "nrhs": nrhs, "N": n, "precision": precision,
+            "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge at FP32); no flush"}
+
+
 def bytes_per_site_rhs(prec: int, n: int, nrhs: int) -> float:
     """Compulsory bytes per output site per RHS: 8 links (N^2 complex each,
     amortised over the RHS) + one input and one output spinor (4N complex)
@@ -448,10 +458,7 @@ def run_gpu(args):
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
-            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(%d), %s, nrhs=%d, %s, antiperiodic t"
-                                   % (n, "x".join(map(str, L)), nrhs, pname.upper()), "lattice": list(L), "nrhs": nrhs,
-                       "N": n, "precision": pname, "parallelism": "replicas (RHS sets independent)" if world > 1 else "1 GPU",
-                       "l2": "inputs larger than L2 (1.2 GB field + 0.6 GB gauge); no flush"},
+            "config": workload_config(L, n, nrhs, world, pname),
             "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
             "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve, "colors": colors,
         }
@@ -709,8 +716,7 @@ def run_reference(args):
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
-            "config": {"workload": "MRHS even-odd Wilson dslash D_eo, SU(3), 32^3x64, nrhs=12, antiperiodic t",
-                       "lattice": list(L), "nrhs": nrhs, "N": n},
+            "config": workload_config(L, n, nrhs, world, "fp64"),
             "cpu_baseline": {"value": value, "unit": "site*RHS/s", "cores": O.num_threads(), "kind": "port",
                              "sample": "one RHS of the 32^3x64 SU(3) workload per step (1/12 of a step), FP64"},
             "e2e": {"value": value, "unit": "site*RHS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
