@@ -42,6 +42,10 @@ struct Shape {
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 tof(double2 a) { return make_float2((float)a.x, (float)a.y); }
 
 template <typename E>
 __device__ __forceinline__ double2 ld(const E* p) {
@@ -98,13 +102,53 @@ __global__ void axpby_kernel(const double2* __restrict__ a, const void* __restri
     acc[i] = 0.0;
   }
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < s.nchunks; c += stride) {
+  if constexpr (PX == PREC_SINGLE && PY == PREC_SINGLE) {
+    // FP32 fields: FP32 arithmetic (the FP64 pipe of this GPU is a small
+    // fraction of the FP32 one); the norm's per-thread sum stays FP64
+    float2 fa[R], fb[R];
 #pragma unroll
     for (int i = 0; i < R; i++) {
-      const int64_t e = c * R + i;
-      const double2 v = cmul(ca[i], ld(x + e)) + cmul(cb[i], ld(y + e));
-      st(y + e, v);
-      if (NORM) acc[i] += v.x * v.x + v.y * v.y;
+      fa[i] = tof(ca[i]);
+      fb[i] = tof(cb[i]);
+    }
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < s.nchunks; c += stride) {
+      float2 xs[R], ys[R];
+      if constexpr (R == 2) {  // one 16-byte vector per operand (chunks are 16-byte aligned)
+        const float4 xq = reinterpret_cast<const float4*>(x)[c], yq = reinterpret_cast<const float4*>(y)[c];
+        xs[0] = make_float2(xq.x, xq.y);
+        xs[1] = make_float2(xq.z, xq.w);
+        ys[0] = make_float2(yq.x, yq.y);
+        ys[1] = make_float2(yq.z, yq.w);
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+          xs[i] = x[c * R + i];
+          ys[i] = y[c * R + i];
+        }
+      }
+      float2 v[R];
+#pragma unroll
+      for (int i = 0; i < R; i++) {
+        const float2 u = cmulf(fa[i], xs[i]), w = cmulf(fb[i], ys[i]);
+        v[i] = make_float2(u.x + w.x, u.y + w.y);
+        if (NORM) acc[i] += (double)fmaf(v[i].x, v[i].x, v[i].y * v[i].y);
+      }
+      if constexpr (R == 2) {
+        reinterpret_cast<float4*>(y)[c] = make_float4(v[0].x, v[0].y, v[1].x, v[1].y);
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; i++) y[c * R + i] = v[i];
+      }
+    }
+  } else {
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < s.nchunks; c += stride) {
+#pragma unroll
+      for (int i = 0; i < R; i++) {
+        const int64_t e = c * R + i;
+        const double2 v = cmul(ca[i], ld(x + e)) + cmul(cb[i], ld(y + e));
+        st(y + e, v);
+        if (NORM) acc[i] += v.x * v.x + v.y * v.y;
+      }
     }
   }
   if (NORM) {
@@ -130,11 +174,53 @@ __global__ void axpbypcz_kernel(const double2* __restrict__ a, const void* __res
     cc[i] = c ? c[g * R + i] : make_double2(1.0, 0.0);
   }
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.nchunks; k += stride) {
+  if constexpr (P == PREC_SINGLE) {  // FP32 fields: FP32 arithmetic
+    float2 fa[R], fb[R], fc[R];
 #pragma unroll
     for (int i = 0; i < R; i++) {
-      const int64_t e = k * R + i;
-      st(z + e, cmul(ca[i], ld(x + e)) + cmul(cb[i], ld(y + e)) + cmul(cc[i], ld(z + e)));
+      fa[i] = tof(ca[i]);
+      fb[i] = tof(cb[i]);
+      fc[i] = tof(cc[i]);
+    }
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.nchunks; k += stride) {
+      float2 xs[R], ys[R], zs[R];
+      if constexpr (R == 2) {
+        const float4 xq = reinterpret_cast<const float4*>(x)[k], yq = reinterpret_cast<const float4*>(y)[k],
+                     zq = reinterpret_cast<const float4*>(z)[k];
+        xs[0] = make_float2(xq.x, xq.y);
+        xs[1] = make_float2(xq.z, xq.w);
+        ys[0] = make_float2(yq.x, yq.y);
+        ys[1] = make_float2(yq.z, yq.w);
+        zs[0] = make_float2(zq.x, zq.y);
+        zs[1] = make_float2(zq.z, zq.w);
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+          xs[i] = x[k * R + i];
+          ys[i] = y[k * R + i];
+          zs[i] = z[k * R + i];
+        }
+      }
+      float2 o[R];
+#pragma unroll
+      for (int i = 0; i < R; i++) {
+        const float2 u = cmulf(fa[i], xs[i]), v = cmulf(fb[i], ys[i]), w = cmulf(fc[i], zs[i]);
+        o[i] = make_float2(u.x + v.x + w.x, u.y + v.y + w.y);
+      }
+      if constexpr (R == 2) {
+        reinterpret_cast<float4*>(z)[k] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+      } else {
+#pragma unroll
+        for (int i = 0; i < R; i++) z[k * R + i] = o[i];
+      }
+    }
+  } else {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.nchunks; k += stride) {
+#pragma unroll
+      for (int i = 0; i < R; i++) {
+        const int64_t e = k * R + i;
+        st(z + e, cmul(ca[i], ld(x + e)) + cmul(cb[i], ld(y + e)) + cmul(cc[i], ld(z + e)));
+      }
     }
   }
 }
@@ -208,7 +294,12 @@ Shape make_shape(const FieldRef& f, int R) {
   return s;
 }
 
-int pick_r(const FieldRef& f) { return (f.prec == PREC_SINGLE && f.nrhs % 2 == 0) ? 2 : 1; }
+// two complex FP32 elements (one 16-byte vector) per thread when nrhs is even
+// and every operand is 16-byte aligned
+int pick_r(const FieldRef& f, const void* other = nullptr, const void* third = nullptr) {
+  const uintptr_t al = (uintptr_t)f.data | (uintptr_t)other | (uintptr_t)third;
+  return (f.prec == PREC_SINGLE && f.nrhs % 2 == 0 && al % 16 == 0) ? 2 : 1;
+}
 
 // block size: a multiple of both G (so the RHS of a thread is fixed) and 32
 int block_size(int G) {
@@ -237,7 +328,7 @@ void Blas::axpby(const double2* a, const FieldRef& x, const double2* b, const Fi
   check_field(x);
   check_field(y);
   QCU_REQUIRE(x.n == y.n && x.nrhs == y.nrhs, QCU_ERR_INVALID_ARGUMENT, "axpby: shape mismatch");
-  const int R = (x.prec == y.prec) ? pick_r(x) : 1;
+  const int R = (x.prec == y.prec) ? pick_r(x, y.data) : 1;
   Shape s = make_shape(x, R);
   const int B = block_size(s.G);
   QCU_REQUIRE(B <= 1024, QCU_ERR_UNSUPPORTED, "nrhs too large for BLAS block");
@@ -261,7 +352,7 @@ void Blas::axpby_norm(const double2* a, const FieldRef& x, const double2* b, con
   check_field(y);
   QCU_REQUIRE(x.n == y.n && x.nrhs == y.nrhs && x.prec == y.prec, QCU_ERR_INVALID_ARGUMENT,
               "axpby_norm: shape/precision mismatch");
-  const int R = pick_r(x);
+  const int R = pick_r(x, y.data);
   Shape s = make_shape(x, R);
   const int B = block_size(s.G);
   QCU_REQUIRE(B <= 1024, QCU_ERR_UNSUPPORTED, "nrhs too large for BLAS block");
@@ -283,7 +374,7 @@ void Blas::axpbypcz(const double2* a, const FieldRef& x, const double2* b, const
   check_field(x);
   QCU_REQUIRE(x.prec == y.prec && y.prec == z.prec && x.n == y.n && y.n == z.n, QCU_ERR_INVALID_ARGUMENT,
               "axpbypcz: shape/precision mismatch");
-  const int R = pick_r(x);
+  const int R = pick_r(x, y.data, z.data);
   Shape s = make_shape(x, R);
   const int B = block_size(s.G);
   QCU_REQUIRE(B <= 1024, QCU_ERR_UNSUPPORTED, "nrhs too large for BLAS block");
