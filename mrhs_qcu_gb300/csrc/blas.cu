@@ -225,7 +225,9 @@ __global__ void axpbypcz_kernel(const double2* __restrict__ a, const void* __res
   }
 }
 
-template <int PX, int PY, int R, int MODE>  // MODE 0: |x|^2, 1: <x, y>
+// MODE 0: |x|^2, 1: <x, y>.  FAST (FP32 fields): the products in FP32, summed
+// in FP64; otherwise every product is formed in FP64 (exact for FP32 inputs).
+template <int PX, int PY, int R, int MODE, bool FAST = false>
 __global__ void reduce_kernel(const void* __restrict__ xv, const void* __restrict__ yv, Shape s, void* partials) {
   using EX = typename V2<typename BT<PX>::real>::t;
   using EY = typename V2<typename BT<PY>::real>::t;
@@ -239,8 +241,13 @@ __global__ void reduce_kernel(const void* __restrict__ xv, const void* __restric
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.nchunks; k += stride) {
 #pragma unroll
       for (int i = 0; i < R; i++) {
-        const double2 v = ld(x + k * R + i);
-        acc[i] += v.x * v.x + v.y * v.y;
+        if constexpr (FAST) {
+          const float2 v = reinterpret_cast<const float2*>(x)[k * R + i];
+          acc[i] += (double)fmaf(v.x, v.x, v.y * v.y);
+        } else {
+          const double2 v = ld(x + k * R + i);
+          acc[i] += v.x * v.x + v.y * v.y;
+        }
       }
     }
     __shared__ double sm[1024 * 2];
@@ -252,9 +259,16 @@ __global__ void reduce_kernel(const void* __restrict__ xv, const void* __restric
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < s.nchunks; k += stride) {
 #pragma unroll
       for (int i = 0; i < R; i++) {
-        const double2 u = ld(x + k * R + i), v = ld(y + k * R + i);
-        acc[i].x += u.x * v.x + u.y * v.y;  // conj(u) v
-        acc[i].y += u.x * v.y - u.y * v.x;
+        if constexpr (FAST) {
+          const float2 u = reinterpret_cast<const float2*>(x)[k * R + i];
+          const float2 v = reinterpret_cast<const float2*>(y)[k * R + i];
+          acc[i].x += (double)fmaf(u.x, v.x, u.y * v.y);  // conj(u) v
+          acc[i].y += (double)fmaf(u.x, v.y, -u.y * v.x);
+        } else {
+          const double2 u = ld(x + k * R + i), v = ld(y + k * R + i);
+          acc[i].x += u.x * v.x + u.y * v.y;  // conj(u) v
+          acc[i].y += u.x * v.y - u.y * v.x;
+        }
       }
     }
     __shared__ double2 sm2[1024 * 2];
@@ -262,13 +276,23 @@ __global__ void reduce_kernel(const void* __restrict__ xv, const void* __restric
   }
 }
 
+// one warp per RHS: lane l sums the block partials l, l + 32, ... in order,
+// then a fixed shuffle tree adds the lanes (deterministic)
 template <typename A>
 __global__ void finalize_kernel(const A* __restrict__ partials, int nblocks, int nrhs, A* out) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrhs) return;
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (r >= nrhs) return;  // whole warps leave together
   A s = A{};
-  for (int b = 0; b < nblocks; b++) s = s + partials[(int64_t)b * nrhs + r];
-  out[r] = s;
+  for (int b = lane; b < nblocks; b += 32) s = s + partials[(int64_t)b * nrhs + r];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) s = s + shfl_xor(s, off);
+  if (lane == 0) out[r] = s;
+}
+
+// launch of finalize_kernel: 4 RHS (warps) per block
+template <typename A>
+void finalize(const A* partials, int nblocks, int nrhs, A* out, cudaStream_t st) {
+  finalize_kernel<A><<<(nrhs + 3) / 4, 128, 0, st>>>(partials, nblocks, nrhs, out);
 }
 
 template <int PX, int PY>
@@ -365,7 +389,7 @@ void Blas::axpby_norm(const double2* a, const FieldRef& x, const double2* b, con
   else
     axpby_kernel<PREC_SINGLE, PREC_SINGLE, 1, true><<<grid, B, 0, st>>>(a, x.data, b, y.data, s, partials_);
   QCU_CHECK_CUDA(cudaGetLastError());
-  finalize_kernel<double><<<(x.nrhs + 127) / 128, 128, 0, st>>>(partials_, grid, x.nrhs, out);
+  finalize<double>(partials_, grid, x.nrhs, out, st);
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -388,7 +412,7 @@ void Blas::axpbypcz(const double2* a, const FieldRef& x, const double2* b, const
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 
-void Blas::norm2(const FieldRef& x, double* out, cudaStream_t st) {
+void Blas::norm2(const FieldRef& x, double* out, cudaStream_t st, bool exact) {
   check_field(x);
   const int R = pick_r(x);
   Shape s = make_shape(x, R);
@@ -397,12 +421,16 @@ void Blas::norm2(const FieldRef& x, double* out, cudaStream_t st) {
   const int grid = grid_for(s.nchunks, B);
   if (x.prec == PREC_DOUBLE)
     reduce_kernel<PREC_DOUBLE, PREC_DOUBLE, 1, 0><<<grid, B, 0, st>>>(x.data, x.data, s, partials_);
-  else if (R == 2)
+  else if (R == 2 && exact)
     reduce_kernel<PREC_SINGLE, PREC_SINGLE, 2, 0><<<grid, B, 0, st>>>(x.data, x.data, s, partials_);
-  else
+  else if (R == 2)
+    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 2, 0, true><<<grid, B, 0, st>>>(x.data, x.data, s, partials_);
+  else if (exact)
     reduce_kernel<PREC_SINGLE, PREC_SINGLE, 1, 0><<<grid, B, 0, st>>>(x.data, x.data, s, partials_);
+  else
+    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 1, 0, true><<<grid, B, 0, st>>>(x.data, x.data, s, partials_);
   QCU_CHECK_CUDA(cudaGetLastError());
-  finalize_kernel<double><<<(x.nrhs + 127) / 128, 128, 0, st>>>(partials_, grid, x.nrhs, out);
+  finalize<double>(partials_, grid, x.nrhs, out, st);
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -421,11 +449,11 @@ void Blas::cdot(const FieldRef& x, const FieldRef& y, double2* out, cudaStream_t
   if (x.prec == PREC_DOUBLE)
     reduce_kernel<PREC_DOUBLE, PREC_DOUBLE, 1, 1><<<grid, B, 0, st>>>(x.data, y.data, s, p2);
   else if (R == 2)
-    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 2, 1><<<grid, B, 0, st>>>(x.data, y.data, s, p2);
+    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 2, 1, true><<<grid, B, 0, st>>>(x.data, y.data, s, p2);
   else
-    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 1, 1><<<grid, B, 0, st>>>(x.data, y.data, s, p2);
+    reduce_kernel<PREC_SINGLE, PREC_SINGLE, 1, 1, true><<<grid, B, 0, st>>>(x.data, y.data, s, p2);
   QCU_CHECK_CUDA(cudaGetLastError());
-  finalize_kernel<double2><<<(x.nrhs + 127) / 128, 128, 0, st>>>(p2, grid, x.nrhs, out);
+  finalize<double2>(p2, grid, x.nrhs, out, st);
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 

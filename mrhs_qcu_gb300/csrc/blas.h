@@ -4,8 +4,9 @@
 //
 // A field is `n` complex elements in RHS-innermost order, so element e
 // belongs to RHS e % nrhs.  Coefficients are per-RHS device arrays of
-// double2 (complex); reductions accumulate in FP64 and return per-RHS
-// results into device arrays, in a fixed order (deterministic).
+// double2 (complex).  FP32 fields are updated in FP32 arithmetic and FP64
+// fields in FP64.  Reductions accumulate in FP64 and return per-RHS results
+// into device arrays, in a fixed order (deterministic).
 #pragma once
 
 #include "qcu_common.cuh"
@@ -32,9 +33,11 @@ class Blas {
   // y = a_r x + b_r y, then out[r] = |y_r|^2 (double)
   void axpby_norm(const double2* a, const FieldRef& x, const double2* b, const FieldRef& y, double* out,
                   cudaStream_t st);
-  // out[r] = |x_r|^2
-  void norm2(const FieldRef& x, double* out, cudaStream_t st);
-  // out[r] = <x_r, y_r> = sum conj(x) y  (double2)
+  // out[r] = |x_r|^2; exact: every product formed in FP64 (exact for FP32
+  // inputs), else FP32 fields form their products in FP32 (summed in FP64)
+  void norm2(const FieldRef& x, double* out, cudaStream_t st, bool exact = true);
+  // out[r] = <x_r, y_r> = sum conj(x) y  (double2); FP32 fields form the
+  // products in FP32, summed in FP64
   void cdot(const FieldRef& x, const FieldRef& y, double2* out, cudaStream_t st);
   // hi += lo (any BLAS precisions), elementwise
   void add_to(const FieldRef& lo, const FieldRef& hi, cudaStream_t st);

@@ -399,7 +399,7 @@ void SlotEngine::cg_iteration() {
     convert_field(op_, qop_.data, qop_.norm, kp_, ql_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
     convert_field(op_, wop_.data, wop_.norm, kp_, wl_.data, nullptr, s_.geo.vh, 4 * s_.N, n_, st_, S_.active);
   }
-  B.norm2(ref(ql_), S_.qq, st_);
+  B.norm2(ref(ql_), S_.qq, st_, false);
   cg_alpha_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
   B.axpby(S_.alpha, ref(pl_), nullptr, ref(xl_), st_);                  // x += a p
   B.axpby_norm(S_.nalpha, ref(ql_), nullptr, ref(sl_), S_.ss, st_);      // s -= a q
@@ -416,7 +416,7 @@ void SlotEngine::bicg_iteration() {
   B.axpby(S_.nalpha, ref(ql_), nullptr, ref(sl_), st_);  // s = r - alpha v (sl holds r)
   op_apply(wl_, sl_, 0, S_.active);                       // t = Mhat s
   B.cdot(ref(wl_), ref(sl_), S_.tmp1, st_);
-  B.norm2(ref(wl_), S_.qq, st_);
+  B.norm2(ref(wl_), S_.qq, st_, false);
   bicg_omega_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
   B.axpbypcz(S_.alpha, ref(pl_), S_.omega, ref(sl_), nullptr, ref(xl_), st_);  // x += alpha p + omega s
   B.axpby_norm(S_.nomega, ref(wl_), nullptr, ref(sl_), S_.ss, st_);            // r = s - omega t
@@ -509,7 +509,7 @@ void SlotEngine::restart(const std::vector<int>& slots, bool fresh) {
   B.axpby(S_.cm, ref(sh_), S_.ck, ref(sl_), st_);  // s_lo = s
   if (q_.solver == 0) {
     op_apply(rl_, sl_, 1, S_.sel);  // r = Mhat^dag s
-    B.norm2(ref(rl_), S_.rr_new, st_);
+    B.norm2(ref(rl_), S_.rr_new, st_, false);
     B.cdot(ref(rl_), ref(pl_), S_.tmp1, st_);
     restart_kernel<<<1, QCU_MAX_RHS, 0, st_>>>(S_, n_);
     B.axpby(S_.tmp2, ref(rl_), nullptr, ref(pl_), st_);  // p += c r
