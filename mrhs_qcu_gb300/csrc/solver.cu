@@ -469,10 +469,15 @@ void SlotEngine::restart(const std::vector<int>& slots, bool fresh) {
     B.axpby(S_.zero, ref(xh_), S_.ck, ref(xh_), st_);  // x = 0
     B.axpby(S_.zero, ref(pl_), S_.ck, ref(pl_), st_);  // p = 0
   }
-  // s = bhat - Mhat x  (only the selected slots are computed)
-  apply_mhat(th_, xh_, tmp64_, tmp64b_, 0, S_.sel);
+  // s = bhat - Mhat x  (only the selected slots are computed); fresh slots
+  // start from x = 0, so their true residual is bhat itself
   B.axpby(S_.cm, ref(bh_), S_.ck, ref(sh_), st_);
-  B.axpby_norm(S_.cn, ref(th_), nullptr, ref(sh_), S_.ss_true, st_);
+  if (fresh) {
+    B.norm2(ref(sh_), S_.ss_true, st_);
+  } else {
+    apply_mhat(th_, xh_, tmp64_, tmp64b_, 0, S_.sel);
+    B.axpby_norm(S_.cn, ref(th_), nullptr, ref(sh_), S_.ss_true, st_);
+  }
   std::vector<double> ss(n_);
   QCU_CHECK_CUDA(cudaMemcpyAsync(ss.data(), S_.ss_true, sizeof(double) * n_, cudaMemcpyDeviceToHost, st_));
   std::vector<int> act(n_);
