@@ -723,6 +723,36 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def profile_solve(inner):
+    """The config-2 solve alone: one cold solve (tuning, graph capture), then
+    a warm one inside the NVTX range 'warm_solve'; prints its wall time."""
+    import torch
+
+    import mrhs_qcu_gb300 as Q
+    from mrhs_qcu_gb300 import synthetic as S
+    L, n, nrhs, kappa = (24, 24, 24, 48), 3, 12, 0.12
+    g_dev, _ = make_inputs(torch, L, n, 1, seed_g=5)
+    b = S.point_sources(L, n, nrhs, seed=6)
+    db = [torch.from_numpy(b[r]).cuda() for r in range(nrhs)]
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    Q.loadQcuGauge(g_dev.data_ptr())
+    for phase in ("cold", "warm"):
+        dx = [torch.zeros_like(x) for x in db]
+        p = Q.solver_params(kappa=kappa, tol=1e-10, inner_precision=inner, max_iter=20000)
+        torch.cuda.synchronize()
+        if phase == "warm":
+            torch.cuda.nvtx.range_push("warm_solve")
+        t0 = time.perf_counter()
+        Q.invert([x.data_ptr() for x in dx], [x.data_ptr() for x in db], p, raise_on_error=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if phase == "warm":
+            torch.cuda.nvtx.range_pop()
+        print(json.dumps({"solve": phase, "inner_precision": inner, "seconds": round(dt, 4),
+                          "iterations": p.iterations, "reliable_updates": p.reliable_updates}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -742,7 +772,13 @@ def main():
     ap.add_argument("--precision", type=int, default=1, help="0 fp16, 1 fp32, 2 fp64, 4 bf16")
     ap.add_argument("--profile", action="store_true",
                     help="headline kernel only (no e2e, sweep, CPU or solve legs), for ncu captures")
+    ap.add_argument("--profile-solve", type=int, default=None, metavar="INNER",
+                    help="only the 24^3x48 mixed solve with this inner precision (0 fp16, 1 fp32, 2 fp64): "
+                         "a cold solve, then a warm one inside the NVTX range 'warm_solve', for ncu captures")
     args = ap.parse_args()
+    if args.profile_solve is not None:
+        profile_solve(args.profile_solve)
+        return
     if args.profile:
         args.skip_sweep = args.skip_solve = args.skip_serve = args.skip_colors = args.skip_cpu = True
         args.skip_e2e = True
