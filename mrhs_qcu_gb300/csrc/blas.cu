@@ -140,6 +140,17 @@ __global__ void axpby_kernel(const double2* __restrict__ a, const void* __restri
         for (int i = 0; i < R; i++) y[c * R + i] = v[i];
       }
     }
+  } else if (b == nullptr) {
+    // b = 1: no multiply of y (FP64 arithmetic is bound by the FP64 pipe here)
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < s.nchunks; c += stride) {
+#pragma unroll
+      for (int i = 0; i < R; i++) {
+        const int64_t e = c * R + i;
+        const double2 v = cmul(ca[i], ld(x + e)) + ld(y + e);
+        st(y + e, v);
+        if (NORM) acc[i] += v.x * v.x + v.y * v.y;
+      }
+    }
   } else {
     for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < s.nchunks; c += stride) {
 #pragma unroll
