@@ -648,45 +648,77 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
   const uint32_t lf = p * NN * vh + site;
   const uint32_t lb = (1u - p) * NN * vh;
   const uint32_t dmu = 2 * NN * vh;  // one direction's links
-  const uint32_t pl = A.geo.plane, cb = A.geo.cube;
-  const bool top = t == Lt - 1, bot = t == 0;
-  // neighbour of hop h: X+, X-, Y+, Y-, Z+, Z-, T+, T-
-  auto nbr = [&](int h) -> uint32_t {
-    switch (h) {
-      case 0: return (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
-      case 1: return (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-      case 2: return (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
-      case 3: return (y == 0) ? site + (Ly - 1) * hx : site - hx;
-      case 4: return (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
-      case 5: return (z == 0) ? site + (Lz - 1) * pl : site - pl;
-      case 6: return top ? site - (Lt - 1) * cb : site + cb;
-      default: return bot ? site + (Lt - 1) * cb : site - cb;
-    }
-  };
-  // Each link is read once per launch, so every hop's link comes from DRAM.
-  // Prefetching all eight into L1 here, with no registers held, leaves the
-  // hops waiting only on their neighbour spinors (mostly L2 hits); the
-  // R-groups of a site split the link components between them.  Measured
-  // faster for FP32 and BF16 storage (4-19%); FP64 is bound by its FMA pipe
-  // and FP16 (with its norm loads) measured 2-6% slower, so they skip it.
+  // FP32 and BF16 storage prefetch every hop's links (below; measured 4-19%
+  // faster).  FP64 is bound by its FMA pipe and FP16 (with its norm loads)
+  // measured 2-6% slower with the prefetch, so they run the hops without it,
+  // in the form that compiles best for them.
   if constexpr (P == PREC_SINGLE || P == PREC_BF16) {
+    const uint32_t pl = A.geo.plane, cb = A.geo.cube;
+    const bool top = t == Lt - 1, bot = t == 0;
+    // neighbour of hop h: X+, X-, Y+, Y-, Z+, Z-, T+, T-
+    auto nbr = [&](int h) -> uint32_t {
+      switch (h) {
+        case 0: return (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+        case 1: return (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+        case 2: return (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
+        case 3: return (y == 0) ? site + (Ly - 1) * hx : site - hx;
+        case 4: return (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
+        case 5: return (z == 0) ? site + (Lz - 1) * pl : site - pl;
+        case 6: return top ? site - (Lt - 1) * cb : site + cb;
+        default: return bot ? site + (Lt - 1) * cb : site - cb;
+      }
+    };
+    // Each link is read once per launch, so every hop's link comes from DRAM.
+    // Prefetching all eight into L1 here, with no registers held, leaves the
+    // hops waiting only on their neighbour spinors (mostly L2 hits); the
+    // R-groups of a site split the link components between them.
     for (uint32_t k = grp; k < NN; k += A.div_groups.d) {
 #pragma unroll
       for (int h = 0; h < 8; h++)
         prefetch_l1(gauge + ((h >> 1) * dmu + ((h & 1) ? lb + nbr(h) : lf) + k * vh));
     }
-  }
-  hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nbr(0), rhs0, (T)1, f);
-  hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbr(1), nbr(1), rhs0, (T)1, f);
-  hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nbr(2), rhs0, (T)1, f);
-  hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbr(3), nbr(3), rhs0, (T)1, f);
-  hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nbr(4), rhs0, (T)1, f);
-  hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbr(5), nbr(5), rhs0, (T)1, f);
-  {  // T, with the optional antiperiodic sign
-    const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
-    const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
-    hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nbr(6), rhs0, bcf, f);
-    hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbr(7), nbr(7), rhs0, bcb, f);
+    hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nbr(0), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbr(1), nbr(1), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nbr(2), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbr(3), nbr(3), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nbr(4), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbr(5), nbr(5), rhs0, (T)1, f);
+    {  // T, with the optional antiperiodic sign
+      const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
+      const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
+      hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nbr(6), rhs0, bcf, f);
+      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbr(7), nbr(7), rhs0, bcb, f);
+    }
+  } else {
+    {  // X
+      const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+      const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+      hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbk, nbk, rhs0, (T)1, f);
+    }
+    {  // Y
+      const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
+      const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
+      hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    }
+    {  // Z
+      const uint32_t pl = A.geo.plane;
+      const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
+      const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
+      hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbk, nbk, rhs0, (T)1, f);
+    }
+    {  // T, with the optional antiperiodic sign
+      const uint32_t cb = A.geo.cube;
+      const bool top = t == Lt - 1, bot = t == 0;
+      const uint32_t nf = top ? site - (Lt - 1) * cb : site + cb;
+      const uint32_t nbk = bot ? site + (Lt - 1) * cb : site - cb;
+      const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
+      const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
+      hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
+      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbk, nbk, rhs0, bcb, f);
+    }
   }
 
   C2<T> acc[4][N][R];
