@@ -10,7 +10,7 @@ compared, and the reference's outputs are written as fixtures:
   seeded random complex projections of each output RHS, its L2 norm, and its
   first sites in full.
 
-Usage:  python tests/golden/make_golden.py [outdir]   (default gpurun_out/golden)
+Usage:  python tests/golden/make_golden.py OUTDIR
 The committed copies live in tests/golden/ beside this script.
 """
 from __future__ import annotations
@@ -136,4 +136,6 @@ def main(outdir: str) -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "gpurun_out", "golden")))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py OUTDIR")
+    sys.exit(main(sys.argv[1]))
