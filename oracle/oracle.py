@@ -1,7 +1,7 @@
 """ctypes wrapper of the FP64 CPU oracle (``oracle/qcu_oracle.c``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline leg of ``bench.py`` as the checker.  The product library
+and the CPU-baseline leg of ``bench.py``, to check results.  The product library
 (``mrhs_qcu_gb300``) never imports it.
 
 Array conventions (all complex128, C-contiguous), restating the reference's

@@ -3,8 +3,8 @@
  * its layout conversions, the clover term and the (Wilson-clover) solve
  * built on them.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
- * smoke check and the CPU-baseline leg of the benchmark load it.  The product
+ * TEST INFRASTRUCTURE ONLY.  The parity tests, the smoke check and the
+ * CPU-baseline leg of the benchmark load it to check results.  The product
  * library never links or calls it and has no CPU fallback.
  *
  * Parity pinning: the dslash here is checked against the reference's own GPU

@@ -1,5 +1,5 @@
 """The multi-rank plumbing of bench.py on CPU: world_size 2 over gloo (one
-process per GPU on a GPU machine; replicas, so the only collectives are the
+process per GPU on one node; replicas, so the only collectives are the
 barrier around the timed region and the max-over-ranks of the step time)."""
 import os
 import socket
