@@ -343,3 +343,31 @@ def test_full_size_fp32_against_oracle(cuda, qcu_lib):
     want = np.einsum("rk,kvsa->rvsa", coef, ref)
     for r in range(12):
         assert rel(got[r], want[r]) < 1e-6
+
+
+def test_queue_batches_and_argument_edges(cuda, qcu_lib):
+    """startDslash with more RHS than one launch takes (300: a batch of 256,
+    then one of 44) against the oracle; a second startDslash on the emptied
+    queue is a no-op; resident calls with no RHS, a null or in-place output or
+    a misaligned field are rejected with QCU_ERR_INVALID_ARGUMENT before any
+    GPU work."""
+    Q = qcu_lib
+    L, n, nrhs = (4, 4, 4, 8), 3, 300
+    g = S.random_gauge(L, n, seed=111)
+    psi = S.random_fermions(L, n, nrhs, seed=112)
+    got = abi_dslash(cuda, Q, psi, g, L, 1, 0, 1, antiperiodic_t=True)
+    assert rel(got, O.dslash(psi, g, L, 1, 0, True)) < TOL[1]
+    Q.clear_error()
+    Q.startDslash(0, 0)
+    assert Q.last_error()[0] == 0
+    db, _ = Q.field_bytes(1, 4)
+    a = cuda.zeros(db // 8 + 2, dtype=cuda.float64, device="cuda")
+    b = cuda.zeros_like(a)
+    for args in ((b.data_ptr(), None, a.data_ptr(), None, 0, 0, 0, 1),
+                 (0, None, a.data_ptr(), None, 4, 0, 0, 1),
+                 (a.data_ptr(), None, a.data_ptr(), None, 4, 0, 0, 1),
+                 (b.data_ptr() + 8, None, a.data_ptr(), None, 4, 0, 0, 1)):
+        with pytest.raises(Q.QcuError) as e:
+            Q.dslash_mrhs(*args)
+        assert e.value.code == 2, args
+    Q.clear_error()
