@@ -196,8 +196,11 @@ def test_against_reference_kernel_same_inputs(cuda, qcu_lib):
     if not ref_runner.available():
         pytest.skip("reference module not built (oracle/build_ref.sh)")
     ref = ref_runner.RefModule()
+    # every instantiation of the reference module (ref_runner.DSLASH_VARIANTS) at least once
     for L, n, nrhs, prec in [((8, 8, 8, 8), 3, 4, "d"), ((8, 4, 4, 8), 3, 5, "d"), ((4, 4, 4, 8), 4, 2, "d"),
-                             ((8, 8, 8, 8), 3, 4, "f"), ((4, 4, 4, 8), 5, 1, "f")]:
+                             ((8, 8, 8, 8), 3, 4, "f"), ((4, 4, 4, 8), 5, 1, "f"), ((8, 4, 4, 8), 3, 1, "d"),
+                             ((4, 8, 4, 8), 3, 2, "d"), ((4, 4, 8, 8), 3, 3, "d"), ((8, 4, 4, 8), 3, 1, "f"),
+                             ((4, 4, 4, 8), 4, 2, "f"), ((4, 4, 4, 8), 5, 1, "d")]:
         g = S.random_gauge(L, n, seed=80)
         psi = S.random_fermions(L, n, nrhs, seed=81)
         for parity, dag, ap in [(0, 0, False), (1, 1, True)]:
