@@ -160,6 +160,36 @@ __device__ __forceinline__ void load_norms(const float* p, float (&nrm)[R]) {
   }
 }
 
+// SU(3) link from its first two rows: row 2 = conj(row 0 x row 1), each real
+// part one multiply and three FMAs (the reference's two-row gauge read,
+// include/kernels/storageLoadStore/loadAndStore.cuh:17-27, completed in
+// registers).  Loads the six stored components at lbase + k * ls_bytes.
+template <typename S, typename T>
+__device__ __forceinline__ void load_su3_two_row(const char* lbase, uint32_t ls_bytes, C2<T> (&u)[3][3]) {
+  using E = typename S::elem;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const auto v = S::to_c(__ldg(reinterpret_cast<const E*>(lbase)));
+    u[k / 3][k % 3].x = (T)v.x;
+    u[k / 3][k % 3].y = (T)v.y;
+    lbase += ls_bytes;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    const int k = (j + 1) % 3, l = (j + 2) % 3;
+    T re = u[0][k].x * u[1][l].x;
+    re = fma(-u[0][k].y, u[1][l].y, re);
+    re = fma(-u[0][l].x, u[1][k].x, re);
+    re = fma(u[0][l].y, u[1][k].y, re);
+    T im = -(u[0][k].x * u[1][l].y);
+    im = fma(-u[0][k].y, u[1][l].x, im);
+    im = fma(u[0][l].x, u[1][k].y, im);
+    im = fma(u[0][l].y, u[1][k].x, im);
+    u[2][j].x = re;
+    u[2][j].y = im;
+  }
+}
+
 // One hop (direction MU, forward or backward) accumulated into acc.
 //   s = -f (forward, projector 1 - f g) or +f (backward, 1 + f g)
 //   kup  = bc * scale_r        multiplies the two upper rows
@@ -236,30 +266,11 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
   C2<T> ul[RC ? 3 : 1][RC ? 3 : 1];
   if constexpr (RC) {
     static_assert(N == 3, "link reconstruction is SU(3) only");
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-      for (int b = 0; b < 3; b++) {
-        const auto v = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)(a * 3 + b) * ls_bytes)));
-        ul[a][b].x = (T)v.x;
-        ul[a][b].y = (T)v.y;
-      }
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      const int k = (j + 1) % 3, l = (j + 2) % 3;
-      ul[2][j].x = (ul[0][k].x * ul[1][l].x - ul[0][k].y * ul[1][l].y) -
-                   (ul[0][l].x * ul[1][k].x - ul[0][l].y * ul[1][k].y);
-      ul[2][j].y = -((ul[0][k].x * ul[1][l].y + ul[0][k].y * ul[1][l].x) -
-                     (ul[0][l].x * ul[1][k].y + ul[0][l].y * ul[1][k].x));
-    }
+    load_su3_two_row<S, T>(lbase, ls_bytes, ul);
   }
 #pragma unroll
   for (int a = 0; a < N; a++) {
     C2<T> t[2][R];
-#pragma unroll
-    for (int u = 0; u < 2; u++)
-#pragma unroll
-      for (int r = 0; r < R; r++) t[u][r].x = t[u][r].y = (T)0;
 #pragma unroll
     for (int b = 0; b < N; b++) {
       // forward uses U[a][b]; backward uses conj(U[b][a])
@@ -278,9 +289,14 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
       for (int u = 0; u < 2; u++)
 #pragma unroll
         for (int r = 0; r < R; r++) {
-          t[u][r].x = fma(ur, h[u][b][r].x, t[u][r].x);
+          if (b == 0) {
+            t[u][r].x = ur * h[u][b][r].x;
+            t[u][r].y = ur * h[u][b][r].y;
+          } else {
+            t[u][r].x = fma(ur, h[u][b][r].x, t[u][r].x);
+            t[u][r].y = fma(ur, h[u][b][r].y, t[u][r].y);
+          }
           t[u][r].x = fma(-ui, h[u][b][r].y, t[u][r].x);
-          t[u][r].y = fma(ur, h[u][b][r].y, t[u][r].y);
           t[u][r].y = fma(ui, h[u][b][r].x, t[u][r].y);
         }
     }
@@ -308,118 +324,148 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 }
 
 // The same hop with FP32 arithmetic on the packed FP32x2 pipe (sm_100+
-// fma.rn.f32x2 through __ffma2_rn).  The two lanes of a packed register hold
-// the two projected spin rows u = 0, 1, which the SU(N) multiply scales by
-// the same link element:
-//   t_re(u=0,1) += (ur, ur) * h_re(u=0,1) + (-ui, -ui) * h_im(u=0,1)
-//   t_im(u=0,1) += (ur, ur) * h_im(u=0,1) + ( ui,  ui) * h_re(u=0,1)
-// so one complex multiply-add of both rows is four packed FMAs instead of
-// eight.  The accumulator is kept in the same lane order: pair s holds spin
-// rows (2s, 2s+1), real parts in re[s], imaginary parts in im[s].  Every
-// lane performs exactly the FMA sequence of hop(), so the results are
-// bit-identical to it.
-template <int P, int N, int R, int MU, bool FWD>
-__device__ __forceinline__ void hop_pk(float2 (&re)[2][N][R], float2 (&im)[2][N][R], const DslashArgs& A,
+// fma.rn.f32x2), for storage that computes in FP32 (FP32, FP16, BF16).  The
+// two lanes of a packed register hold two right-hand sides, RHS 2q and
+// 2q + 1 of the thread: every quantity of the hop (projected half-spinor,
+// link product, accumulator) is the same for both, and the link element is
+// the same, so the two lanes take one pair of broadcast link values.
+//   tr(q) += (ur, ur) * hr(q) + (-ui, -ui) * hi(q)
+//   ti(q) += (ur, ur) * hi(q) + ( ui,  ui) * hr(q)
+// The spin rows never change lanes, so every reconstruction is packed too.
+// Each lane performs exactly the FMA sequence of hop() for its RHS, so the
+// results are bit-identical to it.  The 4N spinor components are loaded in
+// order with a running pointer (64-bit adds instead of wide multiply-adds).
+template <int P, int N, int R, int MU, bool FWD, bool RC>
+__device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4][N][R / 2], const DslashArgs& A,
                                        const typename Store<P>::elem* __restrict__ in,
                                        const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
                                        uint32_t nb, uint32_t rhs0, float bc, float f) {
   using S = Store<P>;
   using E = typename S::elem;
+  static_assert(R % 2 == 0, "packed arithmetic pairs the RHS of a thread");
+  constexpr int Q = R / 2;
   constexpr int u0p = gperm(MU, 0), u1p = gperm(MU, 1);
   constexpr bool imag = gimag(MU);
   const float s = FWD ? -f : f;
   const uint32_t vh = (uint32_t)A.geo.vh;
   const uint32_t nrhs = (uint32_t)A.nrhs;
 
-  float scale[R];
+  float2 ku[Q];
   if constexpr (S::has_norm) {
     float nr[R];
     load_norms<P, R>(A.in_norm + (nb * nrhs + rhs0), nr);
 #pragma unroll
-    for (int r = 0; r < R; r++) scale[r] = bc * nr[r];
+    for (int q = 0; q < Q; q++) ku[q] = make_float2(bc * nr[2 * q], bc * nr[2 * q + 1]);
   } else {
 #pragma unroll
-    for (int r = 0; r < R; r++) scale[r] = bc;
+    for (int q = 0; q < Q; q++) ku[q] = make_float2(bc, bc);
   }
 
-  // projection (scalar FMAs, written straight into the lanes)
-  float2 hr[N][R], hi[N][R];
-  const uint32_t cs_bytes = vh * nrhs * (uint32_t)sizeof(E);
-  const char* base = reinterpret_cast<const char*>(in + (nb * nrhs + rhs0));
-  const float k0 = s * (float)gsign(MU, 0), k1 = s * (float)gsign(MU, 1);
+  VecBuf<E, R> comp[4 * N];
+  {
+    const uint32_t cs_bytes = vh * nrhs * (uint32_t)sizeof(E);
+    const char* pc = reinterpret_cast<const char*>(in + (nb * nrhs + rhs0));
 #pragma unroll
-  for (int a = 0; a < N; a++) {
-    VecBuf<E, R> p0, p1, q0, q1;
-    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(0 * N + a) * cs_bytes), p0.v);
-    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(1 * N + a) * cs_bytes), p1.v);
-    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u0p * N + a) * cs_bytes), q0.v);
-    Vec<E, R>::load(reinterpret_cast<const E*>(base + (uint64_t)(u1p * N + a) * cs_bytes), q1.v);
-#pragma unroll
-    for (int r = 0; r < R; r++) {
-      const float2 x0 = S::to_c(p0.v[r]), x1 = S::to_c(p1.v[r]);
-      const float2 y0 = S::to_c(q0.v[r]), y1 = S::to_c(q1.v[r]);
-      if constexpr (imag) {
-        hr[a][r].x = fmaf(-k0, y0.y, x0.x);
-        hi[a][r].x = fmaf(k0, y0.x, x0.y);
-        hr[a][r].y = fmaf(-k1, y1.y, x1.x);
-        hi[a][r].y = fmaf(k1, y1.x, x1.y);
-      } else {
-        hr[a][r].x = fmaf(k0, y0.x, x0.x);
-        hi[a][r].x = fmaf(k0, y0.y, x0.y);
-        hr[a][r].y = fmaf(k1, y1.x, x1.x);
-        hi[a][r].y = fmaf(k1, y1.y, x1.y);
-      }
+    for (int c = 0; c < 4 * N; c++) {
+      Vec<E, R>::load(reinterpret_cast<const E*>(pc), comp[c].v);
+      pc += cs_bytes;
     }
   }
+  // projection h_u = psi_u + s g(u) psi_perm(u), scalar FMAs into the lanes
+  float2 hr[2][N][Q], hi[2][N][Q];
+  const float k0 = s * (float)gsign(MU, 0), k1 = s * (float)gsign(MU, 1);
+#pragma unroll
+  for (int a = 0; a < N; a++)
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float2 x0 = S::to_c(comp[0 * N + a].v[r]), x1 = S::to_c(comp[1 * N + a].v[r]);
+      const float2 y0 = S::to_c(comp[u0p * N + a].v[r]), y1 = S::to_c(comp[u1p * N + a].v[r]);
+      float h0r, h0i, h1r, h1i;
+      if constexpr (imag) {
+        h0r = fmaf(-k0, y0.y, x0.x);
+        h0i = fmaf(k0, y0.x, x0.y);
+        h1r = fmaf(-k1, y1.y, x1.x);
+        h1i = fmaf(k1, y1.x, x1.y);
+      } else {
+        h0r = fmaf(k0, y0.x, x0.x);
+        h0i = fmaf(k0, y0.y, x0.y);
+        h1r = fmaf(k1, y1.x, x1.x);
+        h1i = fmaf(k1, y1.y, x1.y);
+      }
+      const int q = r >> 1;
+      if (r & 1) {
+        hr[0][a][q].y = h0r;
+        hi[0][a][q].y = h0i;
+        hr[1][a][q].y = h1r;
+        hi[1][a][q].y = h1i;
+      } else {
+        hr[0][a][q].x = h0r;
+        hi[0][a][q].x = h0i;
+        hr[1][a][q].x = h1r;
+        hi[1][a][q].x = h1i;
+      }
+    }
 
   const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
   const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);
+  C2<float> ul[RC ? 3 : 1][RC ? 3 : 1];
+  if constexpr (RC) {
+    static_assert(N == 3, "link reconstruction is SU(3) only");
+    load_su3_two_row<S, float>(lbase, ls_bytes, ul);
+  }
   const float klo0 = s * (float)gsign(MU, u0p), klo1 = s * (float)gsign(MU, u1p);
 #pragma unroll
   for (int a = 0; a < N; a++) {
-    float2 tr[R], ti[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) tr[r] = ti[r] = make_float2(0.f, 0.f);
+    float2 tr[2][Q], ti[2][Q];
 #pragma unroll
     for (int b = 0; b < N; b++) {
-      const uint32_t comp = FWD ? (a * N + b) : (b * N + a);
-      const float2 uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp * ls_bytes)));
-      const float ui = FWD ? uc.y : -uc.y;
-      const float2 urr = make_float2(uc.x, uc.x), uii = make_float2(ui, ui), nuii = make_float2(-ui, -ui);
-#pragma unroll
-      for (int r = 0; r < R; r++) {
-        tr[r] = __ffma2_rn(urr, hr[b][r], tr[r]);
-        tr[r] = __ffma2_rn(nuii, hi[b][r], tr[r]);
-        ti[r] = __ffma2_rn(urr, hi[b][r], ti[r]);
-        ti[r] = __ffma2_rn(uii, hr[b][r], ti[r]);
+      float ur, uim;  // the stored link element; the backward hop conjugates it
+      if constexpr (RC) {
+        const C2<float> uc = FWD ? ul[a][b] : ul[b][a];
+        ur = uc.x;
+        uim = uc.y;
+      } else {
+        const uint32_t comp_l = FWD ? (a * N + b) : (b * N + a);
+        const float2 uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp_l * ls_bytes)));
+        ur = uc.x;
+        uim = uc.y;
       }
+      // forward: ui = uim, tr -= ui hi, ti += ui hr; backward: ui = -uim
+      const float2 ur2 = make_float2(ur, ur);
+      const float2 up2 = make_float2(uim, uim), un2 = make_float2(-uim, -uim);
+#pragma unroll
+      for (int v = 0; v < 2; v++)
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+          if (b == 0) {
+            tr[v][q] = __fmul2_rn(ur2, hr[v][b][q]);
+            ti[v][q] = __fmul2_rn(ur2, hi[v][b][q]);
+          } else {
+            tr[v][q] = __ffma2_rn(ur2, hr[v][b][q], tr[v][q]);
+            ti[v][q] = __ffma2_rn(ur2, hi[v][b][q], ti[v][q]);
+          }
+          tr[v][q] = __ffma2_rn(FWD ? un2 : up2, hi[v][b][q], tr[v][q]);
+          ti[v][q] = __ffma2_rn(FWD ? up2 : un2, hr[v][b][q], ti[v][q]);
+        }
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-      const float2 ku = make_float2(scale[r], scale[r]);
-      const float kl0 = klo0 * scale[r], kl1 = klo1 * scale[r];
-      re[0][a][r] = __ffma2_rn(ku, tr[r], re[0][a][r]);
-      im[0][a][r] = __ffma2_rn(ku, ti[r], im[0][a][r]);
-      if constexpr (u0p == 2) {  // rows 2, 3 <- t rows 0, 1: lane-aligned
-        if constexpr (imag) {
-          re[1][a][r] = __ffma2_rn(make_float2(-kl0, -kl1), ti[r], re[1][a][r]);
-          im[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), tr[r], im[1][a][r]);
-        } else {
-          re[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), tr[r], re[1][a][r]);
-          im[1][a][r] = __ffma2_rn(make_float2(kl0, kl1), ti[r], im[1][a][r]);
-        }
-      } else {  // rows 3, 2 <- t rows 0, 1: lanes crossed, scalar FMAs
-        if constexpr (imag) {
-          re[1][a][r].y = fmaf(-kl0, ti[r].x, re[1][a][r].y);
-          im[1][a][r].y = fmaf(kl0, tr[r].x, im[1][a][r].y);
-          re[1][a][r].x = fmaf(-kl1, ti[r].y, re[1][a][r].x);
-          im[1][a][r].x = fmaf(kl1, tr[r].y, im[1][a][r].x);
-        } else {
-          re[1][a][r].y = fmaf(kl0, tr[r].x, re[1][a][r].y);
-          im[1][a][r].y = fmaf(kl0, ti[r].x, im[1][a][r].y);
-          re[1][a][r].x = fmaf(kl1, tr[r].y, re[1][a][r].x);
-          im[1][a][r].x = fmaf(kl1, ti[r].y, im[1][a][r].x);
-        }
+    for (int q = 0; q < Q; q++) {
+      const float2 kl0 = make_float2(klo0 * ku[q].x, klo0 * ku[q].y);
+      const float2 kl1 = make_float2(klo1 * ku[q].x, klo1 * ku[q].y);
+      re[0][a][q] = __ffma2_rn(ku[q], tr[0][q], re[0][a][q]);
+      im[0][a][q] = __ffma2_rn(ku[q], ti[0][q], im[0][a][q]);
+      re[1][a][q] = __ffma2_rn(ku[q], tr[1][q], re[1][a][q]);
+      im[1][a][q] = __ffma2_rn(ku[q], ti[1][q], im[1][a][q]);
+      if constexpr (imag) {
+        re[u0p][a][q] = __ffma2_rn(make_float2(-kl0.x, -kl0.y), ti[0][q], re[u0p][a][q]);
+        im[u0p][a][q] = __ffma2_rn(kl0, tr[0][q], im[u0p][a][q]);
+        re[u1p][a][q] = __ffma2_rn(make_float2(-kl1.x, -kl1.y), ti[1][q], re[u1p][a][q]);
+        im[u1p][a][q] = __ffma2_rn(kl1, tr[1][q], im[u1p][a][q]);
+      } else {
+        re[u0p][a][q] = __ffma2_rn(kl0, tr[0][q], re[u0p][a][q]);
+        im[u0p][a][q] = __ffma2_rn(kl0, ti[0][q], im[u0p][a][q]);
+        re[u1p][a][q] = __ffma2_rn(kl1, tr[1][q], re[u1p][a][q]);
+        im[u1p][a][q] = __ffma2_rn(kl1, ti[1][q], im[u1p][a][q]);
       }
     }
   }
@@ -449,26 +495,25 @@ struct HopAcc {
 
 template <typename T, int N, int R>
 struct HopAcc<T, N, R, true> {
-  float2 re[2][N][R], im[2][N][R];
+  float2 re[4][N][R / 2], im[4][N][R / 2];  // lanes: RHS 2q, 2q + 1
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int s = 0; s < 2; s++)
+    for (int s = 0; s < 4; s++)
 #pragma unroll
       for (int a = 0; a < N; a++)
 #pragma unroll
-        for (int r = 0; r < R; r++) re[s][a][r] = im[s][a][r] = make_float2(0.f, 0.f);
+        for (int q = 0; q < R / 2; q++) re[s][a][q] = im[s][a][q] = make_float2(0.f, 0.f);
   }
   __device__ __forceinline__ void to_rows(C2<T> (&acc)[4][N][R]) const {
 #pragma unroll
-    for (int s = 0; s < 2; s++)
+    for (int s = 0; s < 4; s++)
 #pragma unroll
       for (int a = 0; a < N; a++)
 #pragma unroll
         for (int r = 0; r < R; r++) {
-          acc[2 * s][a][r].x = re[s][a][r].x;
-          acc[2 * s][a][r].y = im[s][a][r].x;
-          acc[2 * s + 1][a][r].x = re[s][a][r].y;
-          acc[2 * s + 1][a][r].y = im[s][a][r].y;
+          const int q = r >> 1;
+          acc[s][a][r].x = (r & 1) ? re[s][a][q].y : re[s][a][q].x;
+          acc[s][a][r].y = (r & 1) ? im[s][a][q].y : im[s][a][q].x;
         }
   }
 };
@@ -483,7 +528,7 @@ __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK
                                        uint32_t nb, uint32_t rhs0, typename Store<P>::real bc,
                                        typename Store<P>::real f) {
   if constexpr (PK)
-    hop_pk<P, N, R, MU, FWD>(acc.re, acc.im, A, in, gauge, link_off, nb, rhs0, bc, f);
+    hop_pk<P, N, R, MU, FWD, RC>(acc.re, acc.im, A, in, gauge, link_off, nb, rhs0, bc, f);
   else
     hop<P, N, R, MU, FWD, RC>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
 }
@@ -520,11 +565,14 @@ __device__ __forceinline__ void store_out(C2<typename Store<P>::real> (&acc)[4][
   }
   const uint32_t cs = vh * nrhs;
   const uint32_t o = site * nrhs + rhs0;
+  // a plain D application (a = 1, no x): the accumulator is the result
+  const bool plain = !xin && (sizeof(T) == 4 ? (!A.a_rhs_f && A.af == 1.f) : (!A.a_rhs_d && A.a == 1.0));
 #pragma unroll
   for (int sp = 0; sp < 4; sp++)
 #pragma unroll
     for (int a = 0; a < N; a++) {
       const uint32_t off = o + (uint32_t)(sp * N + a) * cs;
+      if (plain) continue;
       if (xin) {
         VecBuf<E, R> xv;
         Vec<E, R>::load(xin + off, xv.v);
@@ -603,7 +651,8 @@ struct RegCap {
       MINB == 2 ? 128 : MINB == 3 ? 85 : MINB == 4 ? 112 : MINB == 5 ? 96 : MINB == 6 ? 104 : 255;
 };
 
-// PK: FP32 arithmetic on the packed FP32x2 pipe (FP32 / 16-bit storage only).
+// PK: FP32 arithmetic on the packed FP32x2 pipe, two RHS per packed register
+// (FP32 / 16-bit storage, even R).
 // RC: SU(3) links read as their first two rows (gauge12), the third reconstructed.
 template <int P, int N, int R, int MINB, bool PK, bool RC = false>
 __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashArgs A) {
@@ -612,7 +661,7 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
   using E = typename S::elem;
   using namespace detail;
   static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
-  static_assert(!(PK && RC), "no packed variant with link reconstruction");
+  static_assert(!PK || R % 2 == 0, "packed arithmetic pairs the RHS of a thread");
 
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, grp;

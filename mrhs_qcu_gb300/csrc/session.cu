@@ -147,8 +147,8 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   float best_ms = 1e30f;
   for (int i = 0; i < n; i++) {
     if (A.nrhs % opts[i]) continue;
-    for (int v = 0; v < 3; v++) {  // plain, packed FP32x2, two-row links
-    const int pk = v == 1, rc = v == 2;
+    for (int v = 0; v < 4; v++) {  // scalar / packed FP32x2 arithmetic x full / two-row links
+    const int pk = v & 1, rc = v >> 1;
     if (rc && !A.gauge12) continue;
     int minbs[8];
     const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8, rc);

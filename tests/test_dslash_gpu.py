@@ -58,11 +58,12 @@ def test_colours_and_rhs_counts(cuda, qcu_lib, n, nrhs, prec):
 @pytest.mark.parametrize("L", [(4, 4, 4, 8), (12, 4, 6, 4)])
 def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     """Every compiled shape, pinned in turn, against the oracle: register
-    kernels (R, register cap, packed), TMA-staged kernels (R, stages) and the
-    tensor-core kernel (BF16, N >= 4).  The packed FP32x2 kernels and the
-    staged kernels are bit-identical to the scalar register kernel of the same
-    R (they perform its FMA sequence); the tensor-core kernel rounds its
-    operands to BF16 and meets the 16-bit tolerance."""
+    kernels (R, register cap, packed, two-row links), TMA-staged kernels (R,
+    stages) and the tensor-core kernel (BF16, N >= 4).  The packed FP32x2
+    kernels and the staged kernels are bit-identical to the scalar register
+    kernel of the same R and link form (they perform its FMA sequence); the
+    tensor-core kernel rounds its operands to BF16 and meets the 16-bit
+    tolerance."""
     Q = qcu_lib
     nrhs = 12
     g = S.random_gauge(L, n, seed=70 + n)
@@ -86,8 +87,8 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     for (R, minb, pk, st, rc, d), got in outs.items():
         if pk or st > 0:
             for (r2, m2, p2, s2, rc2, d2), other in outs.items():
-                if r2 == R and d2 == d and not p2 and not s2 and not rc2:
-                    assert np.array_equal(got, other), (R, minb, pk, st, m2, d)
+                if r2 == R and d2 == d and not p2 and not s2 and rc2 == rc:
+                    assert np.array_equal(got, other), (R, minb, pk, st, rc, m2, d)
 
 
 @pytest.mark.parametrize("prec", [2, 1, 4])
