@@ -320,6 +320,7 @@ def run_gpu(args):
                       ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
                        % (pname, n, R, minb, pk, recon, block)),
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
+    rel_err = headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev)
     Q.set_stream(None)
 
     # ---- end to end through the drop-in ABI with host buffers -----------
@@ -459,12 +460,32 @@ def run_gpu(args):
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
             "config": workload_config(L, n, nrhs, world, pname),
-            "roofline": roof, "clocks": clk.summary(), "gpu_launches": args.steps,
+            "roofline": roof, "rel_err": rel_err, "clocks": clk.summary(), "gpu_launches": args.steps,
             "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve, "colors": colors,
         }
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev, checked=2):
+    """Relative L2 error of the benchmarked result against the FP64 oracle:
+    the timed launches' output field, unpacked to the caller layout, for the
+    first `checked` RHS (the oracle runs on the host cores)."""
+    from mrhs_qcu_gb300 import synthetic as S
+    from oracle import oracle as O
+    vh = S.half_volume(L)
+    dsts = [torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
+    Q.unpack_fermions([d.data_ptr() for d in dsts], fout.data_ptr(), nout_p, Q.QCU_SRC_EO_HALF, 0, prec)
+    torch.cuda.synchronize()
+    got = np.stack([dsts[r].cpu().numpy() for r in range(checked)])
+    del dsts
+    ref = O.dslash(psi_dev[:checked].cpu().numpy(), g_dev.cpu().numpy(), L, 0, 0, True)
+    errs = [float(np.linalg.norm(got[r] - ref[r]) / np.linalg.norm(ref[r])) for r in range(checked)]
+    tol = {2: 1e-13, 1: 1e-6, 0: 5e-3, 4: 5e-3}[prec]
+    return {"max": max(errs), "per_rhs": errs, "rhs_checked": checked, "tolerance": tol,
+            "within_tolerance": max(errs) < tol,
+            "against": "FP64 OpenMP oracle on the host, same inputs (D_eo, antiperiodic t)"}
 
 
 def cpu_baseline(g_dev, psi_dev, L, n, budget_s=12.0):

@@ -120,6 +120,34 @@ int qcuCloverMRHS(void *out, void *out_norm, const void *in, const void *in_norm
  * stream. */
 int qcuNorm2MRHS(double *out, const void *field, int precision, int nrhs);
 
+/* BLAS-1 on MRHS fields (no counterpart in the reference, which has no linear
+ * algebra): the operations the solvers are built from, for callers composing
+ * their own iterations.  Fields hold n_elements complex values, RHS innermost
+ * (element e belongs to RHS e % nrhs; n_elements a multiple of nrhs), in
+ * FP32 or FP64 (x_precision, ...).  a, b, c are device arrays of nrhs
+ * complex doubles (re, im) or NULL for 1; out is a device array.
+ *   QCU_BLAS_AXPBY       y = a x + b y
+ *   QCU_BLAS_AXPBYPCZ    z = a x + b y + c z        (one precision)
+ *   QCU_BLAS_AXPBY_NORM  y = a x + b y, out[r] = |y_r|^2 (doubles)
+ *   QCU_BLAS_NORM2       out[r] = |x_r|^2, every product in FP64
+ *   QCU_BLAS_NORM2_FP32  the same with FP32 products for FP32 fields
+ *   QCU_BLAS_CDOT        out[r] = sum conj(x_r) y_r (complex doubles)
+ *   QCU_BLAS_ADD_TO      y += x (any precisions)
+ *   QCU_BLAS_COPY        y = x (with precision conversion)
+ * Reductions accumulate in FP64 in a fixed order (bitwise reproducible).
+ * Needs an initialised session (its workspace holds the block partial sums);
+ * asynchronous on the library stream. */
+#define QCU_BLAS_AXPBY 0
+#define QCU_BLAS_AXPBYPCZ 1
+#define QCU_BLAS_AXPBY_NORM 2
+#define QCU_BLAS_NORM2 3
+#define QCU_BLAS_NORM2_FP32 4
+#define QCU_BLAS_CDOT 5
+#define QCU_BLAS_ADD_TO 6
+#define QCU_BLAS_COPY 7
+int qcuBlasMRHS(int op, const void *a, const void *b, const void *c, const void *x, int x_precision, void *y,
+                int y_precision, void *z, int z_precision, size_t n_elements, int nrhs, void *out);
+
 /* No counterpart in the reference.  The same per-RHS norm for callers that
  * cannot allocate device memory: host callbacks and graph nodes, real-time
  * loops that cannot absorb cudaFree's device-wide synchronisation, processes

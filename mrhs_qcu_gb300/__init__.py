@@ -75,7 +75,7 @@ EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcu
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
                "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
-               "qcuNorm2MRHSNoAlloc", "qcuLoadClover", "qcuCloverMRHS",
+               "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuLoadClover", "qcuCloverMRHS",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
 
@@ -142,6 +142,7 @@ def lib() -> ctypes.CDLL:
         "qcuInvert": ([PP, PP, I, ctypes.POINTER(QcuSolverParam)], I),
         "qcuNorm2MRHS": ([P, P, I, I], I),
         "qcuNorm2MRHSNoAlloc": ([P, P, I, S, I, P], I),
+        "qcuBlasMRHS": ([I, P, P, P, P, I, P, I, P, I, S, I, P], I),
         "qcuServerCreate": ([ctypes.POINTER(ctypes.c_void_p), S, I, I, I], I),
         "qcuServerAddGauge": ([P, I, ctypes.POINTER(I), I, P, I], I),
         "qcuServerSubmit": ([P, I, D, D, I, PP, PP, ctypes.POINTER(ctypes.c_longlong)], I),
@@ -304,6 +305,17 @@ def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: 
 def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:
     """out[r] = |field_r|^2 into a device array of nrhs doubles (qcuNorm2MRHS)."""
     _raise_if(lib().qcuNorm2MRHS(_p(out), _p(field), int(precision), int(nrhs)))
+
+
+BLAS_AXPBY, BLAS_AXPBYPCZ, BLAS_AXPBY_NORM, BLAS_NORM2, BLAS_NORM2_FP32, BLAS_CDOT, BLAS_ADD_TO, BLAS_COPY = range(8)
+
+
+def blas_mrhs(op: int, n_elements: int, nrhs: int, x, x_precision: int, y=None, y_precision: int = 2, z=None,
+              z_precision: int = 2, a=None, b=None, c=None, out=None) -> None:
+    """One BLAS-1 operation on MRHS fields (qcuBlasMRHS); pointers are device
+    addresses (or None), coefficients device arrays of nrhs complex doubles."""
+    _raise_if(lib().qcuBlasMRHS(int(op), _p(a), _p(b), _p(c), _p(x), int(x_precision), _p(y), int(y_precision),
+                                _p(z), int(z_precision), int(n_elements), int(nrhs), _p(out)))
 
 
 def tune_dslash(nrhs: int, precision: int):

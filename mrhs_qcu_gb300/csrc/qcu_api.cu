@@ -431,6 +431,60 @@ int qcuNorm2MRHS(double* out, const void* field, int precision, int nrhs) {
   });
 }
 
+int qcuBlasMRHS(int op, const void* a, const void* b, const void* c, const void* x, int x_precision, void* y,
+                int y_precision, void* z, int z_precision, size_t n_elements, int nrhs, void* out) {
+  return guarded([&] {
+    Session& s = session();
+    QCU_REQUIRE(op >= QCU_BLAS_AXPBY && op <= QCU_BLAS_COPY, QCU_ERR_INVALID_ARGUMENT, "qcuBlasMRHS: bad op");
+    QCU_REQUIRE(nrhs >= 1 && nrhs <= qcu::QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs must be in 1..256");
+    QCU_REQUIRE(n_elements > 0 && n_elements % (size_t)nrhs == 0, QCU_ERR_INVALID_ARGUMENT,
+                "n_elements must be a positive multiple of nrhs");
+    auto field = [&](const void* p, int prec, const char* name) {
+      QCU_REQUIRE(p != nullptr, QCU_ERR_INVALID_ARGUMENT, std::string("qcuBlasMRHS: null ") + name);
+      QCU_REQUIRE(prec == QCU_SINGLE_PRECISION || prec == QCU_DOUBLE_PRECISION, QCU_ERR_UNSUPPORTED,
+                  "BLAS fields are FP32 or FP64");
+      qcu::FieldRef f;
+      f.data = const_cast<void*>(p);
+      f.prec = prec;
+      f.n = (int64_t)n_elements;
+      f.nrhs = nrhs;
+      return f;
+    };
+    const double2* ca = static_cast<const double2*>(a);
+    const double2* cb = static_cast<const double2*>(b);
+    const double2* cc = static_cast<const double2*>(c);
+    qcu::Blas& blas = s.blas();
+    const qcu::FieldRef fx = field(x, x_precision, "x");
+    const bool reduces = op == QCU_BLAS_AXPBY_NORM || op == QCU_BLAS_NORM2 || op == QCU_BLAS_NORM2_FP32 ||
+                         op == QCU_BLAS_CDOT;
+    QCU_REQUIRE(!reduces || out != nullptr, QCU_ERR_INVALID_ARGUMENT, "qcuBlasMRHS: null out");
+    switch (op) {
+      case QCU_BLAS_NORM2:
+      case QCU_BLAS_NORM2_FP32:
+        blas.norm2(fx, static_cast<double*>(out), s.stream(), op == QCU_BLAS_NORM2);
+        break;
+      case QCU_BLAS_AXPBY:
+        blas.axpby(ca, fx, cb, field(y, y_precision, "y"), s.stream());
+        break;
+      case QCU_BLAS_AXPBY_NORM:
+        blas.axpby_norm(ca, fx, cb, field(y, y_precision, "y"), static_cast<double*>(out), s.stream());
+        break;
+      case QCU_BLAS_AXPBYPCZ:
+        blas.axpbypcz(ca, fx, cb, field(y, y_precision, "y"), cc, field(z, z_precision, "z"), s.stream());
+        break;
+      case QCU_BLAS_CDOT:
+        blas.cdot(fx, field(y, y_precision, "y"), static_cast<double2*>(out), s.stream());
+        break;
+      case QCU_BLAS_ADD_TO:
+        blas.add_to(fx, field(y, y_precision, "y"), s.stream());
+        break;
+      default:
+        blas.copy(fx, field(y, y_precision, "y"), s.stream());
+        break;
+    }
+  });
+}
+
 int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, int* count) {
   return guarded_unlocked([&] {
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");

@@ -32,6 +32,23 @@ def available() -> bool:
         os.path.exists(os.path.join(REF_DIR, "qcuref.ptx"))
 
 
+def expected() -> bool:
+    """True when build_ref.sh found the reference sources: the module must
+    then exist, and a missing module is a build failure, not a skip."""
+    return os.path.exists(os.path.join(REF_DIR, "expected"))
+
+
+def require(pytest) -> None:
+    """Skip when the reference was never available to build; fail when it
+    was and the module is missing."""
+    if available():
+        return
+    if expected():
+        pytest.fail("the reference sources were present but oracle/_ref/ holds no module "
+                    "(oracle/build_ref.sh failed)")
+    pytest.skip("reference module not built (oracle/build_ref.sh found no reference sources)")
+
+
 class RefModule:
     def __init__(self):
         import torch

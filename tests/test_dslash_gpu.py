@@ -194,8 +194,7 @@ def test_odd_and_tiny_lattices(cuda, qcu_lib, L):
 
 def test_against_reference_kernel_same_inputs(cuda, qcu_lib):
     from oracle import ref_runner
-    if not ref_runner.available():
-        pytest.skip("reference module not built (oracle/build_ref.sh)")
+    ref_runner.require(pytest)
     ref = ref_runner.RefModule()
     # every instantiation of the reference module (ref_runner.DSLASH_VARIANTS) at least once
     for L, n, nrhs, prec in [((8, 8, 8, 8), 3, 4, "d"), ((8, 4, 4, 8), 3, 5, "d"), ((4, 4, 4, 8), 4, 2, "d"),

@@ -34,8 +34,7 @@ def _ms_per_call(torch, fn, reps=10):
 @pytest.mark.parametrize("prec", ["f", "d"])
 def test_rate_against_reference_kernel(cuda, qcu_lib, prec):
     from oracle import ref_runner
-    if not ref_runner.available():
-        pytest.skip("reference module not built (oracle/build_ref.sh)")
+    ref_runner.require(pytest)
     torch, Q = cuda, qcu_lib
     L, n, nrhs = (32, 32, 32, 64), 3, 4
     vh = S.half_volume(L)
