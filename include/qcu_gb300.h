@@ -46,9 +46,11 @@ typedef enum QcuStatus_e {
 
 /* precision codes: the reference's QCU_PRECISION values
  * (include/qcu_enum.h:4 of the reference) plus BF16 */
+#ifndef QCU_ENUM_H_INCLUDED /* C++ callers of qcu_enum.h have these as enumerators */
 #define QCU_HALF_PRECISION 0
 #define QCU_SINGLE_PRECISION 1
 #define QCU_DOUBLE_PRECISION 2
+#endif
 #define QCU_BF16_PRECISION 4
 
 /* caller fermion address modes for pack/unpack */

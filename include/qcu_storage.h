@@ -1,7 +1,7 @@
 /*
  * qcu_storage.h -- C++ layout-transform API with the reference's exact
- * signatures (include/storage/qcu_storage.h:5-6 and the ShiftDirection enum
- * of include/qcu_enum.h:19-22 of the reference), so C++ callers of
+ * signatures (include/storage/qcu_storage.h:5-6 of the reference; the
+ * ShiftDirection enum is in qcu_enum.h), so C++ callers of
  * qcu::storage::shiftVectorStorage / shiftGaugeStorage link against libqcu.so
  * unchanged.  Same semantics: complex double SU(3), one RHS, caller layout
  * [Vh][4][3] <-> coalesced [12][Vh], gauge [4][2][Vh][9] <-> [4][2][9][Vh];
@@ -9,10 +9,7 @@
  */
 #pragma once
 
-enum ShiftDirection {
-  TO_COALESCE = 0,
-  TO_NON_COALESCE = 1,
-};
+#include "qcu_enum.h"
 
 namespace qcu {
 namespace storage {

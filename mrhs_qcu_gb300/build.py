@@ -19,8 +19,10 @@ LIB = os.path.join(HERE, "libqcu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host symbols are hidden unless a source exports them (the public headers'
+# declarations, wrapped in "#pragma GCC visibility push(default)")
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-              "-I" + CSRC, "-I" + INCLUDE] + ARCH
+              "-Xcompiler", "-fvisibility=hidden", "-I" + CSRC, "-I" + INCLUDE] + ARCH
 
 
 def nvcc() -> str:

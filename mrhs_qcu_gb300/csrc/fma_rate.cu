@@ -8,7 +8,9 @@
 // A data-dependent store keeps the chains live.
 #include <cuda_runtime.h>
 
+#pragma GCC visibility push(default)  // the public header: exported
 #include "../../include/qcu_gb300.h"
+#pragma GCC visibility pop
 #include "qcu_common.cuh"
 
 extern "C" void qcu_record_error(int code, const char* msg);

@@ -453,6 +453,47 @@ double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cu
   return (double)f;
 }
 
+namespace {
+// element e of the MRHS field = (c * vh + site) * nrhs + r; RHS fastest, so a
+// warp writes one contiguous span and reads nrhs short runs
+template <typename E, bool GATHER>
+__global__ void rhs_arrays_kernel(PtrArray arrays, void* field, int64_t n, FastDiv div_nrhs) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t q = (uint64_t)e / div_nrhs.d;
+    const uint32_t r = (uint32_t)(e - (int64_t)q * div_nrhs.d);
+    if (GATHER)
+      static_cast<E*>(field)[e] = static_cast<const E*>(arrays.p[r])[q];
+    else
+      const_cast<E*>(static_cast<const E*>(arrays.p[r]))[q] = static_cast<const E*>(field)[e];
+  }
+}
+
+template <bool GATHER>
+void rhs_arrays(int prec, const PtrArray& arrays, void* field, int64_t vh, int ncomp, int nrhs, cudaStream_t st) {
+  QCU_REQUIRE(prec == PREC_SINGLE || prec == PREC_DOUBLE, QCU_ERR_UNSUPPORTED,
+              "per-RHS arrays are FP32 or FP64");
+  QCU_REQUIRE(nrhs >= 1 && nrhs <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "nrhs out of range");
+  const int64_t n = vh * ncomp * nrhs;
+  const int block = 256;
+  const int grid = (int)std::min<int64_t>((n + block - 1) / block, 152 * 32);
+  const FastDiv d((uint32_t)nrhs);
+  if (prec == PREC_SINGLE)
+    rhs_arrays_kernel<float2, GATHER><<<grid, block, 0, st>>>(arrays, field, n, d);
+  else
+    rhs_arrays_kernel<double2, GATHER><<<grid, block, 0, st>>>(arrays, field, n, d);
+  QCU_CHECK_CUDA(cudaGetLastError());
+}
+}  // namespace
+
+void gather_rhs_arrays(int prec, const PtrArray& src, void* dst, int64_t vh, int ncomp, int nrhs, cudaStream_t st) {
+  rhs_arrays<true>(prec, src, dst, vh, ncomp, nrhs, st);
+}
+
+void scatter_rhs_arrays(int prec, const PtrArray& dst, const void* src, int64_t vh, int ncomp, int nrhs,
+                        cudaStream_t st) {
+  rhs_arrays<false>(prec, dst, const_cast<void*>(src), vh, ncomp, nrhs, st);
+}
+
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st) {
   dim3 block(32, 8);
   dim3 grid((cols + 31) / 32, (rows + 31) / 32);

@@ -53,6 +53,13 @@ double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cu
 constexpr int kTcLinkBytes = 256;
 inline size_t tc_links_bytes(int64_t vh) { return (size_t)2 * 8 * vh * kTcLinkBytes; }
 void gauge_tc_rows_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st);
+// per-RHS coalesced arrays (the reference's internal layout, one [ncomp][vh]
+// complex array per RHS, include/basic_data/qcu_point.cuh:80-88 of the
+// reference) <-> one MRHS field [ncomp][vh][nrhs], FP32 or FP64 (no
+// conversion).  nrhs <= QCU_MAX_RHS.
+void gather_rhs_arrays(int prec, const PtrArray& src, void* dst, int64_t vh, int ncomp, int nrhs, cudaStream_t st);
+void scatter_rhs_arrays(int prec, const PtrArray& dst, const void* src, int64_t vh, int ncomp, int nrhs,
+                        cudaStream_t st);
 // plain complex-double transpose [rows][cols] -> [cols][rows]
 void transpose_c64(const void* src, void* dst, int rows, int cols, cudaStream_t st);
 

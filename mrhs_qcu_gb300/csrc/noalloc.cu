@@ -15,7 +15,9 @@
 // GPU that loads the library until the process exits.
 #include <mutex>
 
+#pragma GCC visibility push(default)  // the public header: exported
 #include "../../include/qcu_gb300.h"
+#pragma GCC visibility pop
 #include "blas.h"
 
 extern "C" void qcu_record_error(int code, const char* msg);

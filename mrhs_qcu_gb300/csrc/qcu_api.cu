@@ -13,8 +13,10 @@
 #include <mutex>
 #include <string>
 
+#pragma GCC visibility push(default)  // the public headers: exported
 #include "../../include/qcu.h"
 #include "../../include/qcu_gb300.h"
+#pragma GCC visibility pop
 #include "dslash_tc.h"
 #include "dslash_tma.h"
 #include "serve.h"
@@ -192,7 +194,7 @@ void getDslash(int dslashType, double mass, int nColors, int nInputs, int floatP
     QCU_REQUIRE(qcu::prec_valid(floatPrecision), QCU_ERR_UNSUPPORTED,
                 "floatPrecision must be 0 (half), 1 (single), 2 (double) or 4 (bf16)");
     QCU_REQUIRE(nInputs >= 0, QCU_ERR_INVALID_ARGUMENT, "nInputs must not be negative");
-    s.dirac.reset(new qcu::DiracWilson(s, mass, nColors, floatPrecision, dslashType));
+    s.dirac.reset(new qcu::WilsonHopOperator(s, mass, nColors, floatPrecision, dslashType));
     s.gauge(floatPrecision);  // convert the resident gauge once
     s.sync();
   });

@@ -1,4 +1,4 @@
-// Session, Dirac and autotuner implementation (see session.h).
+// Session, hop operator and autotuner implementation (see session.h).
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -221,12 +221,12 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
 }
 
 // ---------------------------------------------------------------------------
-void DiracWilson::Dslash(FieldView out, FieldView in, int parity, int dagger, int nInputs) {
+void WilsonHopOperator::Dslash(FieldView out, FieldView in, int parity, int dagger, int nInputs) {
   QCU_REQUIRE(out.nrhs == nInputs && in.nrhs == nInputs, QCU_ERR_INVALID_ARGUMENT, "Dslash: nInputs mismatch");
   s_.hop(out, in, FieldView{}, parity, dagger, 1.0, 0.0);
 }
 
-void DiracWilson::DslashXpay(FieldView out, FieldView in, FieldView x, int parity, int dagger, int nInputs, double a,
+void WilsonHopOperator::DslashXpay(FieldView out, FieldView in, FieldView x, int parity, int dagger, int nInputs, double a,
                              double b) {
   QCU_REQUIRE(out.nrhs == nInputs && in.nrhs == nInputs && x.nrhs == nInputs, QCU_ERR_INVALID_ARGUMENT,
               "DslashXpay: nInputs mismatch");

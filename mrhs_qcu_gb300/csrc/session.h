@@ -2,10 +2,12 @@
 //
 // Mirrors the reference's host layer: qcu::Qcu (src/qcu.cu:17-123 of the
 // reference) -> Session; qcu::Dirac / DiracWilson (include/qcu_dirac.h:7-50,
-// src/qcu_dirac.cu:7-14) -> Dirac / DiracWilson; QcuLattDesc / QcuProcDesc
-// (include/qcuDesc/qcu_desc.h:9-97) -> LattDesc / ProcDesc; ExecutionStreams
-// (include/qcu_kernel_param.cuh:9-38) -> one library stream created on first
-// use (the reference creates nine streams during static initialisation).
+// src/qcu_dirac.cu:7-14) -> HopOperator / WilsonHopOperator on resident
+// fields; QcuLattDesc / QcuProcDesc (include/qcuDesc/qcu_desc.h:9-97) ->
+// LattDesc / ProcDesc; ExecutionStreams (include/qcu_kernel_param.cuh:9-38)
+// -> one library stream created on first use (the reference creates nine
+// streams during static initialisation).  The reference's own C++ classes,
+// with their signatures, are exported from dirac_api.cu.
 //
 // Resources are cached: the gauge is converted once per precision, and MRHS
 // work buffers are allocated once and reused (the reference allocates and
@@ -88,11 +90,15 @@ struct FieldView {
   int nrhs = 0;
 };
 
-class Dirac {
+// The operator getDslash selects (the reference's Dirac / DiracWilson of
+// include/qcu_dirac.h:7-50, which the public C++ interface of libqcu.so
+// mirrors in include/qcu_dirac.h); internally it works on resident MRHS
+// fields of a session.
+class HopOperator {
  public:
-  Dirac(Session& s, double mass, int nColors, int prec, int type)
+  HopOperator(Session& s, double mass, int nColors, int prec, int type)
       : s_(s), mass_(mass), kappa_(1.0 / (2.0 * (4.0 + mass))), nColors_(nColors), prec_(prec), type_(type) {}
-  virtual ~Dirac() = default;
+  virtual ~HopOperator() = default;
   // out = D_parity^f in for nInputs RHS of the internal MRHS fields
   virtual void Dslash(FieldView out, FieldView in, int parity, int dagger, int nInputs) = 0;
   // out = a * D in + b * x
@@ -109,9 +115,9 @@ class Dirac {
   int nColors_, prec_, type_;
 };
 
-class DiracWilson : public Dirac {
+class WilsonHopOperator : public HopOperator {
  public:
-  using Dirac::Dirac;
+  using HopOperator::HopOperator;
   void Dslash(FieldView out, FieldView in, int parity, int dagger, int nInputs) override;
   void DslashXpay(FieldView out, FieldView in, FieldView x, int parity, int dagger, int nInputs, double a,
                   double b) override;
@@ -128,7 +134,7 @@ class Session {
   Geometry geo;
   int N;
   bool antiperiodic_t = false;
-  std::unique_ptr<Dirac> dirac;
+  std::unique_ptr<HopOperator> dirac;
   std::vector<std::pair<void*, void*>> queue;  // (out, in) caller pointers
   Workspace ws;
   Autotuner& tuner;

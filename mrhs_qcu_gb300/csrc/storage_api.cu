@@ -2,8 +2,10 @@
 // signatures and semantics (src/storage/qcu_storage.cu:9-35 of the
 // reference), implemented as shared-memory tiled transposes.  Errors are
 // reported through qcuGetLastError() instead of exit(1).
+#pragma GCC visibility push(default)  // the public headers: exported
 #include "../../include/qcu_gb300.h"
 #include "../../include/qcu_storage.h"
+#pragma GCC visibility pop
 #include "layout.h"
 
 extern "C" void qcu_record_error(int code, const char* msg);

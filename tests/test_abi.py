@@ -89,3 +89,70 @@ def test_errors_are_reported_not_fatal(lib):
 def test_solver_param_defaults(lib):
     p = Q.solver_params()
     assert p.solver == Q.QCU_SOLVER_CG and p.tol == 1e-10 and p.inner_precision == 1 and p.use_graph == 1
+
+
+# ---- the reference's C++ operator interface (qcu_dirac.h, qcd/qcu_dslash.h) ----
+# mangled names of the reference's declarations (include/qcu_dirac.h:40-50,
+# include/qcd/qcu_dslash.h:62-64 of the reference), which a C++ caller built
+# against the reference's headers links to
+REFERENCE_CXX_SYMBOLS = [
+    "_ZN3qcu17instantiateDslashERK11QcuLattDescILi4EERK11QcuProcDescILi4EEiidPvS8_S8_11DSLASH_TYPE"
+    "13QCU_PRECISIONiiRNS_16ExecutionStreamsE",
+    "_ZN3qcu11DiracWilson6DslashEPvS1_iii",
+    "_ZTVN3qcu11DiracWilsonE",
+    "_ZN3qcu12WilsonDslashIfLi3ELi4EE5applyEv",
+    "_ZN3qcu12WilsonDslashIdLi5ELi1EE5applyEv",
+]
+
+
+def test_reference_operator_symbols_exported(lib):
+    for sym in REFERENCE_CXX_SYMBOLS:
+        assert hasattr(lib, sym), sym
+
+
+def _exported_symbols():
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--defined-only", Q.lib()._name], capture_output=True, text=True).stdout
+    return [line.split()[-1] for line in out.splitlines() if line.strip()]
+
+
+def test_internal_symbols_hidden():
+    """Only the public headers' functions and classes leave libqcu.so: no
+    internal qcu:: symbol (session, solver engine, kernel launchers) is
+    exported, so they cannot clash with a caller's symbols."""
+    syms = _exported_symbols()
+    internal = [s for s in syms if s.startswith("_ZN3qcu") and not (
+        s.startswith("_ZN3qcu17instantiateDslash") or s.startswith("_ZN3qcu11DiracWilson") or
+        s.startswith("_ZN3qcu12WilsonDslash") or s.startswith("_ZN3qcu6Dslash") or
+        s.startswith("_ZN3qcu7storage"))]
+    assert not internal, internal[:10]
+    assert any(s == "initGridSize" for s in syms)
+
+
+def test_cxx_caller_builds_against_public_headers(tmp_path):
+    """A C++ program written against include/ (qcu_dirac.h, qcd/qcu_dslash.h,
+    qcu_gb300.h) compiles with g++ and links against libqcu.so."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if gxx is None or not os.path.exists(os.path.join(cuda, "include", "cuda_runtime.h")):
+        pytest.skip("g++ or the CUDA headers are not available")
+    exe = build_cxx_caller(str(tmp_path), gxx, cuda)
+    assert os.path.exists(exe)
+
+
+def build_cxx_caller(outdir, gxx, cuda):
+    import subprocess
+    libdir = os.path.dirname(Q.lib()._name)
+    exe = os.path.join(outdir, "dirac_caller")
+    cmd = [gxx, "-std=c++17", "-O1", "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(cuda, "include"),
+           os.path.join(ROOT, "tests", "cxx", "dirac_caller.cpp"), "-o", exe, os.path.join(libdir, "libqcu.so"),
+           "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
