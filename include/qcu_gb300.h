@@ -257,8 +257,24 @@ int qcuServerStats(void *server, QcuServerStats *stats);
 int qcuServerDestroy(void *server);
 
 void qcuSolverParamDefaults(QcuSolverParam *p);
-/* Solve M x_r = b_r for nrhs right-hand sides with the loaded gauge. */
+/* Solve M x_r = b_r for nrhs right-hand sides with the loaded gauge.
+ * Returns QCU_ERR_NOT_CONVERGED when some RHS did not reach tol within
+ * max_iter (p->converged[r] and p->true_residual[r] say which), and
+ * QCU_ERR_INVALID_ARGUMENT when a source holds NaN or Inf: such a source is
+ * not solved (its x is not meaningful) while the others are.  The server
+ * reports the same two conditions in QcuRequestInfo.status. */
 int qcuInvert(void *const *x, void *const *b, int nrhs, QcuSolverParam *p);
+
+/* Diagnostic of the device-side wait bound (no counterpart in the
+ * reference).  The staged and tensor-core dslash kernels wait on mbarriers
+ * with a bound of about one second; when a wait runs out, the kernel sets a
+ * device flag and returns, and the next synchronising call reports
+ * QCU_ERR_DEVICE_TIMEOUT with the context still usable.  This runs one
+ * kernel that waits, with the same bounded wait, on a barrier that nothing
+ * completes, with the bound set to limit_seconds (0 < limit_seconds <= 1),
+ * and reports through the same path: the expected result is
+ * QCU_ERR_DEVICE_TIMEOUT.  Synchronous. */
+int qcuCheckWaitTimeout(double limit_seconds);
 
 #ifdef __cplusplus
 }

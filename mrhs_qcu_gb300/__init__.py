@@ -75,7 +75,7 @@ EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcu
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
                "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
-               "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuLoadClover", "qcuCloverMRHS",
+               "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuCheckWaitTimeout", "qcuLoadClover", "qcuCloverMRHS",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
 
@@ -143,6 +143,7 @@ def lib() -> ctypes.CDLL:
         "qcuNorm2MRHS": ([P, P, I, I], I),
         "qcuNorm2MRHSNoAlloc": ([P, P, I, S, I, P], I),
         "qcuBlasMRHS": ([I, P, P, P, P, I, P, I, P, I, S, I, P], I),
+        "qcuCheckWaitTimeout": ([D], I),
         "qcuServerCreate": ([ctypes.POINTER(ctypes.c_void_p), S, I, I, I], I),
         "qcuServerAddGauge": ([P, I, ctypes.POINTER(I), I, P, I], I),
         "qcuServerSubmit": ([P, I, D, D, I, PP, PP, ctypes.POINTER(ctypes.c_longlong)], I),
@@ -300,6 +301,12 @@ def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: 
                      a: float, b: float) -> None:
     _raise_if(lib().qcuDslashXpayMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), _p(x), _p(x_norm), int(nrhs),
                                       int(parity), int(dagger), int(precision), float(a), float(b)))
+
+
+def check_wait_timeout(limit_seconds: float) -> int:
+    """Run the device-side bounded-wait diagnostic (qcuCheckWaitTimeout);
+    returns its status code, QCU_ERR_DEVICE_TIMEOUT (9) when the bound works."""
+    return lib().qcuCheckWaitTimeout(float(limit_seconds))
 
 
 def norm2_mrhs(out, field, precision: int, nrhs: int) -> None:

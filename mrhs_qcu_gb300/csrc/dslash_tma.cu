@@ -69,6 +69,33 @@ int* tma_error_flag() {
 
 void tma_note_launch() { g_launched.store(true, std::memory_order_relaxed); }
 
+namespace {
+// one warp; lane 0 waits on phase 0 of a barrier that expects one arrival
+// and never gets it, so the bounded wait runs out, sets the flag and returns
+__global__ void wait_selftest_kernel(int* err, uint64_t limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = tma::smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    tma::mbar_init(b, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    tma::mbar_wait(b, 0, err, limit_ns);
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(b) : "memory");
+  }
+}
+}  // namespace
+
+bool wait_timeout_selftest(double limit_s, cudaStream_t st) {
+  int* flag = tma_error_flag();
+  wait_selftest_kernel<<<1, 32, 0, st>>>(flag, (uint64_t)(limit_s * 1e9));
+  QCU_CHECK_CUDA(cudaGetLastError());
+  tma_note_launch();
+  QCU_CHECK_CUDA(cudaStreamSynchronize(st));
+  return tma_check_timeout(st);
+}
+
 bool tma_check_timeout(cudaStream_t st) {
   if (!g_launched.exchange(false)) return false;
   int* flag = tma_error_flag();

@@ -67,12 +67,13 @@ __device__ __forceinline__ uint64_t now_ns() {
   return t;
 }
 
-// Wait until the phase with the given parity has completed; false after about
-// one second (then *err is set).  After the first poll the warp is suspended
-// in try_wait (suspend-time hint) until the phase completes or the hint runs
-// out, so waiting warps take no issue slots from working ones; the clock is
-// read every 16 polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+// Wait until the phase with the given parity has completed; false after
+// about limit_ns nanoseconds (default one second; then *err is set).  After
+// the first poll the warp is suspended in try_wait (suspend-time hint) until
+// the phase completes or the hint runs out, so waiting warps take no issue
+// slots from working ones; the clock is read every 16 polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err,
+                                          uint64_t limit_ns = 1000000000ull) {
   uint32_t ok = 0;
   asm volatile(
       "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -88,7 +89,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* er
         : "r"(bar), "r"(parity), "r"(1000000u)
         : "memory");
     if (ok) return true;
-    if ((i & 15u) == 0 && now_ns() - t0 > 1000000000ull) {
+    if ((i & 15u) == 0 && now_ns() - t0 > limit_ns) {
       atomicExch(err, 1);
       return false;
     }

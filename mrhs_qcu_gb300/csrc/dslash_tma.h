@@ -16,6 +16,10 @@ int* tma_error_flag();
 // since the last check (synchronises the stream first)
 bool tma_check_timeout(cudaStream_t st);
 void tma_note_launch();
+// One kernel whose bounded wait (limit_s seconds) is on an mbarrier that
+// nothing completes: the timeout path of the staged kernels, without any
+// copy in flight.  Returns whether the device reported the timeout.
+bool wait_timeout_selftest(double limit_s, cudaStream_t st);
 
 // tensor maps in 4-byte units: field [4N][Vh][nrhs] with box {rcta, hx, 4N};
 // gauge [8][N*N][Vh] with box {hx, N*N, 1}

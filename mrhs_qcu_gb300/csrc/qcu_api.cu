@@ -487,6 +487,16 @@ int qcuBlasMRHS(int op, const void* a, const void* b, const void* c, const void*
   });
 }
 
+int qcuCheckWaitTimeout(double limit_seconds) {
+  return guarded([&] {
+    QCU_REQUIRE(limit_seconds > 0.0 && limit_seconds <= 1.0, QCU_ERR_INVALID_ARGUMENT,
+                "qcuCheckWaitTimeout: limit_seconds must be in (0, 1]");
+    const bool timed_out = qcu::wait_timeout_selftest(limit_seconds, 0);
+    QCU_REQUIRE(!timed_out, QCU_ERR_DEVICE_TIMEOUT,
+                "a device-side wait gave up after its bound (diagnostic kernel; the context stays usable)");
+  });
+}
+
 int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, int* count) {
   return guarded_unlocked([&] {
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -655,11 +665,15 @@ int qcuInvert(void* const* x, void* const* b, int nrhs, QcuSolverParam* p) {
     p->reliable_updates = r.reliable_updates;
     p->seconds = r.seconds;
     bool all = true;
+    std::string bad;
     for (int i = 0; i < nrhs && i < 256; i++) {
       p->true_residual[i] = r.true_residual[i];
       p->converged[i] = r.converged[i];
       all &= r.converged[i] != 0;
+      if (r.bad_source[i]) bad += (bad.empty() ? "" : ", ") + std::to_string(i);
     }
+    QCU_REQUIRE(bad.empty(), QCU_ERR_INVALID_ARGUMENT,
+                "qcuInvert: source(s) " + bad + " hold NaN or Inf; they were not solved (the others were)");
     QCU_REQUIRE(all, QCU_ERR_NOT_CONVERGED, "qcuInvert: not every RHS converged");
   });
 }

@@ -77,6 +77,12 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::qcu::Error((code), (msg));      \
   } while (0)
 
+// Host-side fault injection for the failure tests: when the environment
+// variable QCU_INJECT_FAILURE names this site ("session": creating a session,
+// "solver": creating a solver engine), a host allocation failure is raised
+// there, which the C ABI reports as QCU_ERR_OUT_OF_MEMORY.
+void inject_failure(const char* site);
+
 // ---------------------------------------------------------------------------
 // fast unsigned division by a runtime constant (round-up multiplier method):
 // for d >= 1 and n < 2^31, q = umulhi(n, m) >> s with s = ceil(log2 d) and

@@ -277,17 +277,19 @@ void Server::Impl::run_lane(Lane* L) {
         r->finished++;
         if (r->finished == r->nrhs) {
           eng.retire(r->slots, r->x.data(), mode);
+          bool bad_source = false;
           for (int t : r->slots) {
             const SlotState& h = eng.slot(t);
             r->iterations = std::max(r->iterations, h.iterations);
             r->max_res = std::max(r->max_res, std::sqrt(h.true_res2 / h.bb));
             r->all_converged &= h.converged;
+            bad_source |= h.bad_source != 0;
             L->owner.erase(t);
           }
           std::lock_guard<std::mutex> lk(m);
           r->t_done = Clock::now();
           r->done = true;
-          r->status = r->all_converged ? QCU_OK : QCU_ERR_NOT_CONVERGED;
+          r->status = bad_source ? QCU_ERR_INVALID_ARGUMENT : r->all_converged ? QCU_OK : QCU_ERR_NOT_CONVERGED;
           latencies.push_back(std::chrono::duration<double>(r->t_done - r->t_submit).count());
           completed++;
           rhs_done += r->nrhs;

@@ -2,7 +2,9 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
+#include <new>
 #include <sstream>
 
 #include "session.h"
@@ -17,7 +19,13 @@ void* DeviceBuffer::ensure(size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (bytes > bytes_) {
     release();
-    QCU_CHECK_CUDA(cudaMalloc(&p_, bytes));
+    const cudaError_t e = cudaMalloc(&p_, bytes);
+    if (e != cudaSuccess) {
+      p_ = nullptr;
+      // clear the runtime's last error, so the next launch check does not report this failure again
+      (void)cudaGetLastError();
+      QCU_CHECK_CUDA(e);
+    }
     bytes_ = bytes;
   }
   return p_;
@@ -33,6 +41,11 @@ size_t Workspace::total_bytes() const {
   size_t s = 0;
   for (auto& kv : bufs_) s += kv.second.bytes();
   return s;
+}
+
+void inject_failure(const char* site) {
+  const char* e = getenv("QCU_INJECT_FAILURE");
+  if (e && strcmp(e, site) == 0) throw std::bad_alloc();
 }
 
 // ---------------------------------------------------------------------------
@@ -235,6 +248,7 @@ void WilsonHopOperator::DslashXpay(FieldView out, FieldView in, FieldView x, int
 
 // ---------------------------------------------------------------------------
 Session::Session(const int L[4], const int grid[4], int nColors) : tuner(global_tuner()) {
+  inject_failure("session");
   for (int i = 0; i < 4; i++) {
     latt.dim[i] = L[i];
     proc.dim[i] = grid ? grid[i] : 1;

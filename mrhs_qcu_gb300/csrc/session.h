@@ -228,6 +228,7 @@ struct SolveResult {
   double seconds = 0.0;
   std::vector<double> true_residual;
   std::vector<int> converged;
+  std::vector<int> bad_source;  // 1: the source held NaN or Inf (not solved)
 };
 SolveResult solve(Session& s, void* const* x, void* const* b, int nrhs, const SolveRequest& req);
 

@@ -232,6 +232,7 @@ size_t SlotEngine::bytes_needed(const Session& s, int capacity, int inner_prec) 
 
 SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const std::string& tag)
     : s_(s), n_(capacity), q_(q) {
+  inject_failure("solver");
   QCU_REQUIRE(capacity >= 1 && capacity <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "slot capacity must be in 1..256");
   QCU_REQUIRE(q.solver == 0 || q.solver == 1, QCU_ERR_INVALID_ARGUMENT, "unknown solver");
   QCU_REQUIRE(prec_valid(q.inner_prec), QCU_ERR_INVALID_ARGUMENT, "bad inner precision");
@@ -558,8 +559,11 @@ void SlotEngine::admit(const std::vector<int>& slots, void* const* b, const doub
   QCU_CHECK_CUDA(cudaStreamSynchronize(st_));
   for (int r : slots) {
     SlotState& h = host_[r];
-    h.bb = bb[r] + bo2[r];
-    if (!(h.bb > 0)) h.bb = 1.0;  // a zero source: x = 0 is exact
+    const double b2 = bb[r] + bo2[r];
+    // a non-finite source is not solved: its true residual is non-finite, so
+    // restart() finishes the slot unconverged, and the caller is told why
+    h.bad_source = std::isfinite(b2) ? 0 : 1;
+    h.bb = (b2 > 0 && std::isfinite(b2)) ? b2 : 1.0;  // a zero source: x = 0 is exact
     h.stop2 = h.tol * h.tol * h.bb;
     stop2[r] = h.stop2;
   }
@@ -647,10 +651,12 @@ SolveResult solve(Session& s, void* const* x, void* const* b, int nrhs, const So
   SolveResult res;
   res.true_residual.resize(nrhs);
   res.converged.resize(nrhs);
+  res.bad_source.resize(nrhs);
   for (int r = 0; r < nrhs; r++) {
     const SlotState& h = eng.slot(r);
     res.true_residual[r] = std::sqrt(h.true_res2 / h.bb);
     res.converged[r] = h.converged;
+    res.bad_source[r] = h.bad_source;
     res.iterations = std::max(res.iterations, h.iterations);
     res.reliable_updates = std::max(res.reliable_updates, h.updates);
   }

@@ -27,6 +27,7 @@ struct SlotState {
   int phase = FREE;
   bool reported = false;
   int converged = 0;
+  int bad_source = 0;  // the source held NaN or Inf: the slot is finished unsolved
   int iterations = 0;
   int updates = 0;
   double kappa = 0.0, tol = 0.0, bb = 1.0, stop2 = 0.0, true_res2 = 0.0;
