@@ -81,21 +81,21 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """Per-launch DRAM bytes of the headline kernel from the committed ncu summary."""
+def profile_traffic(kernel: str):
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum)
+    of exactly this kernel shape on the headline workload, from the committed
+    ncu summary (lines "<bytes> <kernel string>"); None when that shape was
+    not captured."""
     path = os.path.join(ROOT, "profiles", "dslash_traffic.txt")
     if not os.path.exists(path):
         return None
-    out = {}
     with open(path) as fh:
         for line in fh:
             if line.strip() and not line.startswith("#"):
-                k, v = line.split(None, 1)
-                out[k] = v.strip()
-    for k in list(out):
-        if k.startswith("dram_bytes_per_launch"):
-            out[k] = float(out[k])
-    return out
+                v, k = line.split(None, 1)
+                if k.strip() == kernel:
+                    return float(v)
+    return None
 
 
 class ClockSampler:
@@ -306,19 +306,18 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     bpu = bytes_per_site_rhs(prec, n, nrhs)
     achieved = bpu * units / (ms_local * 1e-3) / 1e9
-    traffic = profile_traffic()
+    kernel = (("wilson_tcs_kernel<N=%d,stages=%d> (tcgen05)" % (n, -stages - 2)) if stages <= -4 else
+              ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
+              ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
+              ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
+               % (pname, n, R, minb, pk, recon, block)))
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bpu * units,
-            # measured DRAM bytes of the kernel the tuner picked (profiles/dslash_traffic.txt)
-            "traffic": traffic.get("dram_bytes_per_launch_tma" if stages > 0 else
-                                   "dram_bytes_per_launch_rc" if recon else "dram_bytes_per_launch_reg")
-            if (traffic and tuple(L) == L_BENCH and nrhs == NRHS and prec == 1 and n == NC) else None,
-            "kernel": ("wilson_tcs_kernel<N=%d,stages=%d> (tcgen05)" % (n, -stages - 2)) if stages <= -4 else
-                      ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
-                      ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
-                      ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
-                       % (pname, n, R, minb, pk, recon, block)),
+            # measured DRAM bytes of exactly this kernel shape on this workload (profiles/dslash_traffic.txt)
+            "traffic": profile_traffic(kernel)
+            if (tuple(L) == L_BENCH and nrhs == NRHS and prec == 1 and n == NC) else None,
+            "kernel": kernel,
             "gflops": round(FLOPS_PER_SITE_RHS(n) * units / (ms_local * 1e-3) / 1e9, 1)}
     rel_err = headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev)
     Q.set_stream(None)
@@ -399,8 +398,14 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_same = all(torch.equal(host_out[r], dev_out[0][r].cpu()) for r in range(nrhs))
         bytes_io = nrhs * vh * 4 * n * 16
+        link = host_link_peaks(torch, host_in, host_out, dev_in[0], dev_out[0])
+        # the step moves bytes_io each way over the host link: its bound is the slowest of the
+        # two directions alone and of both directions at once
+        link_ms = max(bytes_io / link["h2d_gbs"], bytes_io / link["d2h_gbs"], 2 * bytes_io / link["both_gbs"]) / 1e6
         e2e = {"value": job_throughput(units, world, ems), "unit": "site*RHS/s", "h2d_bytes_per_step": bytes_io,
                "d2h_bytes_per_step": bytes_io, "ms_per_step": round(ems, 3), "steps": e2e_steps,
+               "host_link": link, "link_bound_ms_per_step": round(link_ms, 3),
+               "frac_of_link_bound": round(link_ms / ems, 4),
                "path": "pinned host -> upload stream -> pushBackFermions x12 + startDslash -> download stream -> "
                        "pinned host (FP64 caller layout); device buffers double buffered so step k+1's upload "
                        "and step k-1's download overlap step k",
@@ -466,6 +471,36 @@ def run_gpu(args):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def host_link_peaks(torch, host_in, host_out, dev_in, dev_out, reps=3):
+    """Copy-engine bandwidth between pinned host memory and the GPU with the
+    e2e leg's own buffers: host->device alone, device->host alone, and both
+    directions at once on two streams (GB/s, best of `reps`)."""
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+    nbytes = sum(t.numel() * t.element_size() for t in host_in)
+
+    def run(up, down):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if up:
+            with torch.cuda.stream(s_up):
+                for h, d in zip(host_in, dev_in):
+                    d.copy_(h, non_blocking=True)
+        if down:
+            with torch.cuda.stream(s_down):
+                for h, d in zip(host_out, dev_out):
+                    h.copy_(d, non_blocking=True)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    out = {}
+    for name, up, down, moved in (("h2d_gbs", 1, 0, nbytes), ("d2h_gbs", 0, 1, nbytes),
+                                  ("both_gbs", 1, 1, 2 * nbytes)):
+        best = min(run(up, down) for _ in range(reps))
+        out[name] = round(moved / best / 1e9, 1)
+    out["how"] = "pinned host <-> device copies of the e2e buffers, best of %d, wall clock" % reps
+    return out
 
 
 def headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev, checked=2):

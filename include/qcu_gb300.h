@@ -163,13 +163,17 @@ int qcuBlasMRHS(int op, const void *a, const void *b, const void *c, const void 
  *   limit:      nrhs <= 64; larger requests return QCU_ERR_CAPACITY
  *   stream:     cudaStream_t (NULL: the legacy default stream), asynchronous
  * The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call shares the one array: calls whose work overlaps on the GPU
- * race, so serialise them (one stream, or events). */
+ * (cudaGetSymbolAddress) and keeps it for the life of the process; make that
+ * first call before any stream capture, and do not use the library on a
+ * device after cudaDeviceReset (which destroys the array).  Every call
+ * shares the one array: calls whose work overlaps on the GPU race, so
+ * serialise them (one stream, or events). */
 int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_elements, int nrhs, void *stream);
 
-/* Pick and cache the fastest kernel shape for (N, nrhs, volume, precision).
- * Returns the chosen RHS-per-thread, block size, register-cap variant
+/* The kernel shape the dslash uses for (N, nrhs, volume, precision): the
+ * shape pinned by QCU_DSLASH_CONFIG, else the cached choice (this process's,
+ * or the file named by QCU_TUNE_CACHE), else the fastest shape, timed now and
+ * cached.  Returns the chosen RHS-per-thread, block size, register-cap variant
  * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
  * 6 = 104), whether the packed FP32x2 arithmetic variant was chosen, and the
  * ring depth of the TMA-staged kernel (0: the register kernel was chosen;

@@ -14,6 +14,8 @@
 // g_noalloc_partials: 1024 blocks x 64 RHS doubles = 512 KiB, held on every
 // GPU that loads the library until the process exits.
 #include <mutex>
+#include <new>
+#include <stdexcept>
 
 #pragma GCC visibility push(default)  // the public header: exported
 #include "../../include/qcu_gb300.h"
@@ -39,7 +41,9 @@ void* g_addr[kMaxDevices] = {};
 // Device address of g_noalloc_partials on the current device.  In host code
 // the array's name is only a host-side stand-in, never a device address, so
 // the address is queried once per device, with that device current, and
-// cached.
+// cached for the life of the process.  cudaDeviceReset destroys the module
+// that holds the array (and every other resource of this library on that
+// device), so the library is not used on a device after resetting it.
 double* partials_address() {
   int dev = -1;
   QCU_CHECK_CUDA(cudaGetDevice(&dev));
@@ -82,5 +86,11 @@ extern "C" int qcuNorm2MRHSNoAlloc(double* out, const void* field, int precision
   } catch (const qcu::Error& e) {
     qcu_record_error(e.code, e.what());
     return e.code;
+  } catch (const std::bad_alloc&) {
+    qcu_record_error(QCU_ERR_OUT_OF_MEMORY, "host allocation failed");
+    return QCU_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    qcu_record_error(QCU_ERR_CUDA, e.what());
+    return QCU_ERR_CUDA;
   }
 }

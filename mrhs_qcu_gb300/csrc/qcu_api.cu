@@ -555,7 +555,10 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     A.parity = 0;
     A.dagger = 0;
     A.antiperiodic_t = 0;
-    qcu::DslashConfig c = s.tuner.tune(A, precision, s.N, s.stream());
+    // the shape the dslash uses: the pinned or cached choice, else tuned now
+    bool found = false;
+    qcu::DslashConfig c = s.tuner.lookup(precision, s.N, nrhs, s.geo.vh, &found);
+    if (!found) c = s.tuner.tune(A, precision, s.N, s.stream());
     if (rhs_per_thread) *rhs_per_thread = c.R;
     if (block) *block = c.block;
     if (min_blocks) *min_blocks = c.minb;
