@@ -448,6 +448,11 @@ def run_gpu(args):
     if rank == 0 and not args.skip_solve:
         solve = solve_bench(torch, Q)
 
+    # ---- one launch over several lattices vs one launch per lattice ------
+    multi = None
+    if rank == 0 and not args.skip_serve:
+        multi = multi_lattice_bench(torch, Q)
+
     # ---- serving stream: continuous batching over resident gauges -------
     serve = None
     if rank == 0 and not args.skip_serve:
@@ -466,7 +471,8 @@ def run_gpu(args):
             "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
             "config": workload_config(L, n, nrhs, world, pname),
             "roofline": roof, "rel_err": rel_err, "clocks": clk.summary(), "gpu_launches": args.steps,
-            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve, "colors": colors,
+            "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve,
+            "multi_lattice": multi, "colors": colors,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -654,7 +660,66 @@ def colors_bench(torch, Q, peak, fma):
             "dslash": rows, "bicgstab": solves}
 
 
-def serve_bench(torch, Q, n_requests=48, rates=(20.0, 60.0, 200.0), serial_budget_s=8.0):
+def multi_lattice_bench(torch, Q, reps=20):
+    """The hop term on a mix of lattices (the serving workload's 8^4,
+    16^3x32 and 24^3x48 SU(3), FP32, various RHS counts, plus sixteen small
+    8^4 segments): one qcuDslashSegments launch over the whole work list
+    against one launch per lattice (each with its own tuned shape), timed with
+    CUDA events on one stream."""
+    from mrhs_qcu_gb300 import synthetic as S
+    n = 3
+    mixes = {"serving_lattices": [((8, 8, 8, 8), 4), ((16, 16, 16, 32), 12), ((24, 24, 24, 48), 24),
+                                  ((16, 16, 16, 32), 8)],
+             "sixteen_8^4": [((8, 8, 8, 8), 4)] * 16}
+    stream = torch.cuda.current_stream()
+    out = {"workload": "D_eo, SU(3), FP32, antiperiodic t; one launch over the work list vs one per lattice"}
+    gen = torch.Generator(device="cuda").manual_seed(77)
+    for name, mix in mixes.items():
+        segs, keep, units = [], [], 0
+        for L, nrhs in mix:
+            vh = S.half_volume(L)
+            g = S.random_sun_torch(4 * 2 * vh, n, gen).view(4, 2, vh, n * n).permute(0, 1, 3, 2)
+            gc = g.to(torch.complex64).contiguous()
+            g12 = gc[:, :, :6, :].contiguous()
+            fin = torch.randn(4 * n * vh * nrhs * 2, generator=gen, device="cuda", dtype=torch.float32)
+            fout = torch.empty_like(fin)
+            keep += [gc, g12, fin, fout]
+            segs.append({"lattice": L, "gauge": gc.data_ptr(), "gauge_two_row": g12.data_ptr(),
+                         "in_": fin.data_ptr(), "out": fout.data_ptr(), "nrhs": nrhs, "antiperiodic_t": True})
+            units += vh * nrhs
+        h = stream.cuda_stream
+
+        def batched():
+            Q.dslash_segments(segs, n, 1, h)
+
+        def separate():
+            for sg in segs:
+                Q.dslash_segments([sg], n, 1, h)
+
+        res = {}
+        for arm, fn in (("one_launch", batched), ("per_lattice", separate)):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res[arm] = {"ms": round(ms, 4), "site_rhs_per_s": round(units / (ms * 1e-3))}
+        res["speedup"] = round(res["per_lattice"]["ms"] / res["one_launch"]["ms"], 3)
+        res["segments"] = len(mix)
+        res["lattices"] = ["%s nrhs %d" % ("x".join(map(str, L)), r) for L, r in mix[:4]] + (
+            ["..."] if len(mix) > 4 else [])
+        out[name] = res
+        del keep
+    torch.cuda.empty_cache()
+    return out
+
+
+def serve_bench(torch, Q, n_requests=48, rates=(5.0, 10.0, 20.0, 60.0, 200.0), serial_budget_s=8.0):
     """Serving stream: the same seeded request set arriving by a Poisson
     process at each rate into a server with 4 resident gauges; p50/p99 latency
     and solves/s per rate, next to serial plain-FP64 solves of the same

@@ -170,6 +170,35 @@ int qcuBlasMRHS(int op, const void *a, const void *b, const void *c, const void 
  * serialise them (one stream, or events). */
 int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_elements, int nrhs, void *stream);
 
+/* One segment of qcuDslashSegments: the hop term on one lattice, with its
+ * own gauge and fields (no counterpart in the reference, which launches one
+ * kernel per operator call). */
+typedef struct QcuHopSegment_s {
+  int lattice[4];              /* X, Y, Z, T of this segment's lattice (X even) */
+  const void *gauge;           /* [4][2][N*N][Vh] complex, the coalesced gauge layout, in `precision` */
+  const void *gauge_two_row;   /* SU(3) only: [4][2][6][Vh], the first two rows of every link, or NULL */
+  const void *in;              /* resident MRHS field [4N][Vh][nrhs] (parity 1 - parity) */
+  void *out;                   /* resident MRHS field, output parity; not the same memory as in or x */
+  const void *x;               /* optional xpay field (output parity), or NULL */
+  double a, b;                 /* out = a * D in + b * x (a = 1, b = 0: the plain hop) */
+  int nrhs, parity, dagger, antiperiodic_t;
+} QcuHopSegment;
+
+/* The hop term on `count` segments of different lattices, gauges and RHS
+ * counts in one kernel launch per 16 segments: a work list of (segment,
+ * block) pairs, so small lattices share the GPU instead of each paying a
+ * launch and a tail.  All segments share one kernel shape (same nColors and
+ * precision, FP32, FP64 or BF16): the one QCU_DSLASH_CONFIG pins, else the
+ * fastest work-list shape for this list of (volume, nrhs), timed on the first
+ * call with it and cached (one segment: the lattice's own tuned shape, as
+ * qcuDslashMRHS uses); each result is bit-identical to launching that shape
+ * on the segment alone.  When the
+ * shape has no work-list form the segments run one launch each, and a
+ * segment whose nrhs is not a multiple of the shape's RHS per thread runs
+ * alone with its own shape.  Asynchronous on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream). */
+int qcuDslashSegments(const QcuHopSegment *segments, int count, int nColors, int precision, void *stream);
+
 /* The kernel shape the dslash uses for (N, nrhs, volume, precision): the
  * shape pinned by QCU_DSLASH_CONFIG, else the cached choice (this process's,
  * or the file named by QCU_TUNE_CACHE), else the fastest shape, timed now and

@@ -75,9 +75,16 @@ EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcu
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
                "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
-               "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuCheckWaitTimeout", "qcuLoadClover", "qcuCloverMRHS",
+               "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuCheckWaitTimeout", "qcuDslashSegments", "qcuLoadClover", "qcuCloverMRHS",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
+
+
+class QcuHopSegment(ctypes.Structure):
+    _fields_ = [("lattice", ctypes.c_int * 4), ("gauge", ctypes.c_void_p), ("gauge_two_row", ctypes.c_void_p),
+                ("in_", ctypes.c_void_p), ("out", ctypes.c_void_p), ("x", ctypes.c_void_p),
+                ("a", ctypes.c_double), ("b", ctypes.c_double), ("nrhs", ctypes.c_int), ("parity", ctypes.c_int),
+                ("dagger", ctypes.c_int), ("antiperiodic_t", ctypes.c_int)]
 
 
 class QcuRequestInfo(ctypes.Structure):
@@ -144,6 +151,7 @@ def lib() -> ctypes.CDLL:
         "qcuNorm2MRHSNoAlloc": ([P, P, I, S, I, P], I),
         "qcuBlasMRHS": ([I, P, P, P, P, I, P, I, P, I, S, I, P], I),
         "qcuCheckWaitTimeout": ([D], I),
+        "qcuDslashSegments": ([ctypes.POINTER(QcuHopSegment), I, I, I, P], I),
         "qcuServerCreate": ([ctypes.POINTER(ctypes.c_void_p), S, I, I, I], I),
         "qcuServerAddGauge": ([P, I, ctypes.POINTER(I), I, P, I], I),
         "qcuServerSubmit": ([P, I, D, D, I, PP, PP, ctypes.POINTER(ctypes.c_longlong)], I),
@@ -301,6 +309,23 @@ def dslash_xpay_mrhs(out, out_norm, inp, in_norm, x, x_norm, nrhs: int, parity: 
                      a: float, b: float) -> None:
     _raise_if(lib().qcuDslashXpayMRHS(_p(out), _p(out_norm), _p(inp), _p(in_norm), _p(x), _p(x_norm), int(nrhs),
                                       int(parity), int(dagger), int(precision), float(a), float(b)))
+
+
+def dslash_segments(segments, n_colors: int, precision: int, stream=None) -> None:
+    """The hop term on several (lattice, gauge, fields) segments in one launch
+    (qcuDslashSegments).  `segments`: dicts with keys lattice, gauge,
+    gauge_two_row (or None), in_, out, x (or None), a, b, nrhs, parity,
+    dagger, antiperiodic_t; pointers are device addresses."""
+    arr = (QcuHopSegment * max(1, len(segments)))()
+    for i, d in enumerate(segments):
+        g = arr[i]
+        g.lattice = (ctypes.c_int * 4)(*d["lattice"])
+        g.gauge, g.gauge_two_row = d["gauge"], d.get("gauge_two_row")
+        g.in_, g.out, g.x = d["in_"], d["out"], d.get("x")
+        g.a, g.b = d.get("a", 1.0), d.get("b", 0.0)
+        g.nrhs, g.parity, g.dagger = d["nrhs"], d.get("parity", 0), d.get("dagger", 0)
+        g.antiperiodic_t = int(bool(d.get("antiperiodic_t", False)))
+    _raise_if(lib().qcuDslashSegments(arr, len(segments), int(n_colors), int(precision), _p(stream)))
 
 
 def check_wait_timeout(limit_seconds: float) -> int:

@@ -1,4 +1,5 @@
 // Dslash registry and launch (see dslash.h).
+#include <algorithm>
 #include <map>
 #include <mutex>
 
@@ -19,7 +20,38 @@ std::mutex& registry_mutex() {
 int key(int prec, int N, int R, int minb, int pk, int rc) {
   return ((((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk) * 2 + rc;
 }
+std::map<int, SegmentsLauncher>& seg_registry() {
+  static std::map<int, SegmentsLauncher> r;
+  return r;
+}
 }  // namespace
+
+void register_segments(int prec, int N, int R, int minb, int pk, int rc, SegmentsLauncher fn) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  seg_registry()[key(prec, N, R, minb, pk, rc)] = fn;
+}
+
+SegmentsLauncher find_segments(int prec, int N, int R, int minb, int pk, int rc) {
+  std::lock_guard<std::mutex> lk(registry_mutex());
+  auto it = seg_registry().find(key(prec, N, R, minb, pk, rc));
+  return it == seg_registry().end() ? nullptr : it->second;
+}
+
+int segments_options(int prec, int N, int* out, int max) {
+  int n = 0;
+  for (int R = 1; R <= 8; R++)
+    for (int m = 1; m <= 7; m++)
+      for (int pk = 0; pk < 2; pk++)
+        for (int rc = 0; rc < 2; rc++)
+          if (n < max && find_segments(prec, N, R, m, pk, rc)) {
+            out[4 * n] = R;
+            out[4 * n + 1] = m;
+            out[4 * n + 2] = pk;
+            out[4 * n + 3] = rc;
+            n++;
+          }
+  return n;
+}
 
 void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
@@ -138,6 +170,57 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
   B.bf = (float)A.b;
   fn(B, cfg.block, st);
   QCU_CHECK_CUDA(cudaGetLastError());
+}
+
+int launch_dslash_segments(const std::vector<DslashArgs>& all, int prec, int N, const DslashConfig& cfg_in,
+                           cudaStream_t st, std::vector<int>* misfits) {
+  DslashConfig cfg = cfg_in;
+  const int R = (cfg.tc || cfg.tma > 0) ? 1 : cfg.R;  // the staged and tensor-core kernels take any nrhs here
+  std::vector<DslashArgs> segs;
+  bool all_rc = true;
+  for (size_t i = 0; i < all.size(); i++) {
+    if (all[i].nrhs % R) {
+      misfits->push_back((int)i);
+      continue;
+    }
+    segs.push_back(all[i]);
+    all_rc &= all[i].gauge12 != nullptr;
+  }
+  if (segs.empty()) return 0;
+  if (cfg.rc && !all_rc) cfg.rc = 0;
+  SegmentsLauncher fn = (cfg.tma <= 0 && cfg.tc == 0) ? find_segments(prec, N, cfg.R, cfg.minb, cfg.pk, cfg.rc)
+                                                      : nullptr;
+  if (!fn) {  // no work-list form of this shape: one launch per segment
+    for (const DslashArgs& A : segs) launch_dslash(A, prec, N, cfg, st);
+    return (int)segs.size();
+  }
+  QCU_REQUIRE(cfg.block >= 32 && cfg.block <= 256 && cfg.block % 32 == 0, QCU_ERR_INVALID_ARGUMENT,
+              "dslash block size must be a multiple of 32 in 32..256");
+  int launches = 0;
+  for (size_t base = 0; base < segs.size(); base += kMaxHopSegments) {
+    HopSegments S;
+    S.count = (int)std::min<size_t>(kMaxHopSegments, segs.size() - base);
+    int64_t blocks = 0;
+    for (int i = 0; i < S.count; i++) {
+      DslashArgs B = segs[base + i];
+      QCU_REQUIRE((int64_t)B.geo.vh * (B.nrhs / cfg.R) < (1ll << 31), QCU_ERR_INVALID_ARGUMENT,
+                  "lattice x nrhs too large for one launch");
+      QCU_REQUIRE((int64_t)4 * N * B.geo.vh * B.nrhs < (1ll << 32) && (int64_t)8 * N * N * B.geo.vh < (1ll << 32),
+                  QCU_ERR_INVALID_ARGUMENT, "field too large for 32-bit element offsets");
+      QCU_REQUIRE((int64_t)B.geo.vh * B.nrhs * prec_complex_bytes(prec) < (1ll << 32), QCU_ERR_INVALID_ARGUMENT,
+                  "field component stride must stay below 4 GB");
+      B.div_groups = FastDiv((uint32_t)(B.nrhs / cfg.R));
+      B.af = (float)B.a;
+      B.bf = (float)B.b;
+      S.A[i] = B;
+      blocks += ((int64_t)B.geo.vh * (B.nrhs / cfg.R) + cfg.block - 1) / cfg.block;
+    }
+    QCU_REQUIRE(blocks < (1ll << 31), QCU_ERR_INVALID_ARGUMENT, "work list too large for one launch");
+    fn(S, cfg.block, st);
+    QCU_CHECK_CUDA(cudaGetLastError());
+    launches++;
+  }
+  return launches;
 }
 
 }  // namespace qcu

@@ -6,6 +6,8 @@
 // groups of R RHS per thread instead of a compile-time 1..5.
 #pragma once
 
+#include <vector>
+
 #include "dslash_kernel.cuh"
 
 namespace qcu {
@@ -43,5 +45,21 @@ bool tc_runs(const DslashArgs& A, int prec, int N, int variant = 1);
 
 // launch with an explicit configuration (throws if not compiled)
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg, cudaStream_t st);
+
+// Work-list form of the register kernel (wilson_segments_kernel): many
+// (lattice, gauge, fields) segments in one launch.
+using SegmentsLauncher = void (*)(HopSegments&, int block, cudaStream_t);
+void register_segments(int prec, int N, int R, int minb, int pk, int rc, SegmentsLauncher fn);
+SegmentsLauncher find_segments(int prec, int N, int R, int minb, int pk, int rc);
+// the shapes with a work-list form for (prec, N): up to max (R, minb, pk, rc) in out[4 * i ..]
+int segments_options(int prec, int N, int* out, int max);
+// The hop on the segments with the kernel shape cfg: those whose nrhs is a
+// multiple of its R run in one launch per kMaxHopSegments segments when the
+// shape has a work-list form (two-row links only when every one of them has
+// them), else one launch each.  The indices of the segments cfg cannot take
+// (nrhs not a multiple of R) are returned in *misfits, not launched.
+// Returns the number of launches.
+int launch_dslash_segments(const std::vector<DslashArgs>& segs, int prec, int N, const DslashConfig& cfg,
+                           cudaStream_t st, std::vector<int>* misfits);
 
 }  // namespace qcu

@@ -651,19 +651,21 @@ struct RegCap {
       MINB == 2 ? 128 : MINB == 3 ? 85 : MINB == 4 ? 112 : MINB == 5 ? 96 : MINB == 6 ? 104 : 255;
 };
 
+namespace detail {
+
+// The work of one thread of the register kernel: output site x R RHS number
+// gid of the launch (gid = site * G + RHS group).
 // PK: FP32 arithmetic on the packed FP32x2 pipe, two RHS per packed register
 // (FP32 / 16-bit storage, even R).
 // RC: SU(3) links read as their first two rows (gauge12), the third reconstructed.
-template <int P, int N, int R, int MINB, bool PK, bool RC = false>
-__global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashArgs A) {
+template <int P, int N, int R, bool PK, bool RC>
+__device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
   using S = Store<P>;
   using T = typename S::real;
   using E = typename S::elem;
-  using namespace detail;
   static_assert(!PK || sizeof(T) == 4, "packed arithmetic is FP32 only");
   static_assert(!PK || R % 2 == 0, "packed arithmetic pairs the RHS of a thread");
 
-  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t site, grp;
   A.div_groups.divmod(gid, site, grp);
   if (site >= (uint32_t)A.geo.vh) return;
@@ -773,7 +775,14 @@ __global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashA
   C2<T> acc[4][N][R];
   hacc.to_rows(acc);
 
-  detail::store_out<P, N, R>(acc, A, site, rhs0);
+  store_out<P, N, R>(acc, A, site, rhs0);
+}
+
+}  // namespace detail
+
+template <int P, int N, int R, int MINB, bool PK, bool RC = false>
+__global__ void __maxnreg__(RegCap<MINB>::regs) wilson_mrhs_kernel(const DslashArgs A) {
+  detail::wilson_site<P, N, R, PK, RC>(A, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // host-side launcher of one instantiation
@@ -783,6 +792,41 @@ void launch_wilson_mrhs(const DslashArgs& A, int block, cudaStream_t stream) {
   const int64_t threads = (int64_t)A.geo.vh * groups;
   const int grid = (int)((threads + block - 1) / block);
   wilson_mrhs_kernel<P, N, R, MINB, PK, RC><<<grid, block, 0, stream>>>(A);
+}
+
+// One launch over a work list of up to kMaxHopSegments segments: each
+// segment is a whole register-kernel launch of its own (lattice, gauge,
+// fields, nrhs, parity, coefficients), and block b of the launch is block
+// b - block_begin[s] of segment s.  Every thread does exactly what it does in
+// the segment's own launch with the same block size, so the results are
+// bit-identical to one launch per segment; small lattices share the GPU
+// instead of each paying a launch and a tail.
+constexpr int kMaxHopSegments = 16;
+struct HopSegments {
+  int count = 0;
+  uint32_t block_begin[kMaxHopSegments + 1];
+  DslashArgs A[kMaxHopSegments];
+};
+
+template <int P, int N, int R, int MINB, bool PK, bool RC = false>
+__global__ void __maxnreg__(RegCap<MINB>::regs) wilson_segments_kernel(const __grid_constant__ HopSegments S) {
+  int s = 0;
+#pragma unroll 1
+  while (s + 1 < S.count && blockIdx.x >= S.block_begin[s + 1]) s++;
+  detail::wilson_site<P, N, R, PK, RC>(S.A[s], (blockIdx.x - S.block_begin[s]) * blockDim.x + threadIdx.x);
+}
+
+// the segments' div_groups must be set (nrhs / R); fills block_begin
+template <int P, int N, int R, int MINB, bool PK = false, bool RC = false>
+void launch_wilson_segments(HopSegments& S, int block, cudaStream_t stream) {
+  uint32_t total = 0;
+  for (int s = 0; s < S.count; s++) {
+    S.block_begin[s] = total;
+    const int64_t threads = (int64_t)S.A[s].geo.vh * (S.A[s].nrhs / R);
+    total += (uint32_t)((threads + block - 1) / block);
+  }
+  S.block_begin[S.count] = total;
+  wilson_segments_kernel<P, N, R, MINB, PK, RC><<<total, block, 0, stream>>>(S);
 }
 
 }  // namespace qcu

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -483,6 +484,133 @@ int qcuBlasMRHS(int op, const void* a, const void* b, const void* c, const void*
       default:
         blas.copy(fx, field(y, y_precision, "y"), s.stream());
         break;
+    }
+  });
+}
+
+namespace {
+// The fastest work-list shape for these segments: every registered
+// work-list form that fits them (nrhs a multiple of R) at block sizes 32, 64,
+// 128, timed on the segments themselves (out = a D in + b x does not read
+// out, so repeating it is harmless).
+qcu::DslashConfig tune_work_list(const std::vector<qcu::DslashArgs>& segs, int prec, int N, cudaStream_t st,
+                                 bool* found) {
+  int opts[4 * 64];
+  const int n = qcu::segments_options(prec, N, opts, 64);
+  qcu::DslashConfig best;
+  float best_ms = 1e30f;
+  *found = false;
+  cudaEvent_t e0, e1;
+  QCU_CHECK_CUDA(cudaEventCreate(&e0));
+  QCU_CHECK_CUDA(cudaEventCreate(&e1));
+  for (int i = 0; i < n; i++) {
+    bool fits = true;
+    for (const qcu::DslashArgs& A : segs) fits &= A.nrhs % opts[4 * i] == 0 && (!opts[4 * i + 3] || A.gauge12);
+    if (!fits) continue;
+    for (int block : {32, 64, 128}) {
+      qcu::DslashConfig c;
+      c.R = opts[4 * i];
+      c.minb = opts[4 * i + 1];
+      c.pk = opts[4 * i + 2];
+      c.rc = opts[4 * i + 3];
+      c.block = block;
+      std::vector<int> misfits;
+      qcu::launch_dslash_segments(segs, prec, N, c, st, &misfits);  // warm-up
+      QCU_CHECK_CUDA(cudaEventRecord(e0, st));
+      for (int k = 0; k < 3; k++) qcu::launch_dslash_segments(segs, prec, N, c, st, &misfits);
+      QCU_CHECK_CUDA(cudaEventRecord(e1, st));
+      QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      QCU_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best_ms) best_ms = ms, best = c, *found = true;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+}  // namespace
+
+int qcuDslashSegments(const QcuHopSegment* segments, int count, int nColors, int precision, void* stream) {
+  return guarded([&] {
+    QCU_REQUIRE(count >= 0 && (segments || count == 0), QCU_ERR_INVALID_ARGUMENT, "qcuDslashSegments: bad list");
+    QCU_REQUIRE(precision == QCU_SINGLE_PRECISION || precision == QCU_DOUBLE_PRECISION ||
+                    precision == QCU_BF16_PRECISION,
+                QCU_ERR_UNSUPPORTED, "qcuDslashSegments: FP32, FP64 or BF16 fields");
+    QCU_REQUIRE(nColors >= 3 && nColors <= 8, QCU_ERR_UNSUPPORTED, "nColors must be in 3..8");
+    if (count == 0) return;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    std::vector<qcu::DslashArgs> segs(count);
+    int big = 0;
+    int64_t big_units = -1;
+    for (int i = 0; i < count; i++) {
+      const QcuHopSegment& g = segments[i];
+      for (int d = 0; d < 4; d++) QCU_REQUIRE(g.lattice[d] > 0, QCU_ERR_INVALID_ARGUMENT, "lattice sizes must be positive");
+      QCU_REQUIRE(g.lattice[0] % 2 == 0, QCU_ERR_INVALID_ARGUMENT, "lattice X extent must be even");
+      QCU_REQUIRE(g.gauge && g.in && g.out && g.out != g.in && g.out != g.x, QCU_ERR_INVALID_ARGUMENT,
+                  "segment " + std::to_string(i) + ": null field, or out the same memory as in or x");
+      QCU_REQUIRE(((uintptr_t)g.in | (uintptr_t)g.out | (uintptr_t)g.x) % 16 == 0, QCU_ERR_INVALID_ARGUMENT,
+                  "fields must be 16-byte aligned");
+      QCU_REQUIRE(g.nrhs >= 1 && (g.parity == 0 || g.parity == 1) && (g.dagger == 0 || g.dagger == 1),
+                  QCU_ERR_INVALID_ARGUMENT, "segment " + std::to_string(i) + ": bad nrhs, parity or dagger");
+      QCU_REQUIRE(!g.gauge_two_row || nColors == 3, QCU_ERR_INVALID_ARGUMENT, "two-row links are SU(3) only");
+      qcu::DslashArgs& A = segs[i];
+      A.gauge = g.gauge;
+      A.gauge12 = g.gauge_two_row;
+      A.in = g.in;
+      A.in_norm = nullptr;
+      A.out = g.out;
+      A.out_norm = nullptr;
+      A.x = g.x;
+      A.x_norm = nullptr;
+      A.mask = nullptr;
+      A.a_rhs_f = nullptr;
+      A.a_rhs_d = nullptr;
+      A.a = g.a;
+      A.b = g.b;
+      A.geo = qcu::make_geometry(g.lattice);
+      A.nrhs = g.nrhs;
+      A.parity = g.parity;
+      A.dagger = g.dagger;
+      A.antiperiodic_t = g.antiperiodic_t ? 1 : 0;
+      const int64_t units = (int64_t)A.geo.vh * A.nrhs;
+      if (units > big_units) big_units = units, big = i;
+    }
+    // The shape: pinned by QCU_DSLASH_CONFIG; else the one tuned for this work
+    // list (cached per list); else the largest segment's own shape.
+    qcu::Autotuner& tuner = qcu::global_tuner();
+    bool found = false;
+    const qcu::DslashArgs& B = segs[big];
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QCU_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
+    const bool may_tune = tuner.enabled() && cs == cudaStreamCaptureStatusNone;
+    qcu::DslashConfig c;
+    if (getenv("QCU_DSLASH_CONFIG")) c = tuner.lookup(precision, nColors, B.nrhs, B.geo.vh, &found);
+    if (!found && count > 1) {  // one segment: the lattice's own tuned shape, as for qcuDslashMRHS
+      std::string key = std::to_string(precision) + ":" + std::to_string(nColors);
+      for (const qcu::DslashArgs& A : segs)
+        key += ":" + std::to_string(A.geo.vh) + "x" + std::to_string(A.nrhs) + (A.gauge12 ? "r" : "f");
+      static std::map<std::string, qcu::DslashConfig> tuned_lists;  // under the API lock
+      auto it = tuned_lists.find(key);
+      if (it != tuned_lists.end()) {
+        c = it->second;
+        found = true;
+      } else if (may_tune) {
+        c = tune_work_list(segs, precision, nColors, st, &found);
+        if (found) tuned_lists[key] = c;
+      }
+    }
+    if (!found) {
+      c = tuner.lookup(precision, nColors, B.nrhs, B.geo.vh, &found);
+      if (!found && may_tune) c = tuner.tune(B, precision, nColors, st);
+    }
+    std::vector<int> misfits;
+    qcu::launch_dslash_segments(segs, precision, nColors, c, st, &misfits);
+    for (int i : misfits) {  // an RHS count the shared shape cannot take: the segment's own shape
+      const qcu::DslashArgs& A = segs[i];
+      qcu::DslashConfig own = tuner.lookup(precision, nColors, A.nrhs, A.geo.vh, &found);
+      if (!found && may_tune) own = tuner.tune(A, precision, nColors, st);
+      qcu::launch_dslash(A, precision, nColors, own, st);
     }
   });
 }
