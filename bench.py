@@ -284,7 +284,7 @@ def run_gpu(args):
     nout_p = nout.data_ptr() if nout is not None else None
     ptrs = [psi_dev[r].data_ptr() for r in range(nrhs)]
     Q.pack_fermions(fin.data_ptr(), nin_p, ptrs, Q.QCU_SRC_EO_HALF, 1, prec)
-    R, block, minb, pk, stages, recon = Q.tune_dslash(nrhs, prec)
+    R, block, minb, pk, stages, recon, linktma = Q.tune_dslash(nrhs, prec)
     for _ in range(args.warmup):
         Q.dslash_mrhs(fout.data_ptr(), nout_p, fin.data_ptr(), nin_p, nrhs, 0, 0, prec)
     torch.cuda.synchronize()
@@ -309,6 +309,8 @@ def run_gpu(args):
     kernel = (("wilson_tcs_kernel<N=%d,stages=%d> (tcgen05)" % (n, -stages - 2)) if stages <= -4 else
               ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
               ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
+              ("wilson_tmalink_kernel<%s,N=%d,R=%d,reg_cap=%d,recon=%d> row CTA"
+               % (pname, n, R, minb, recon)) if linktma else
               ("wilson_mrhs_kernel<%s,N=%d,R=%d,reg_cap=%d,PK=%d,recon=%d> block %d"
                % (pname, n, R, minb, pk, recon, block)))
     roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -646,7 +648,7 @@ def colors_bench(torch, Q, peak, fma):
                          raise_on_error=False)
                 torch.cuda.synchronize()
                 sec = time.perf_counter() - t0
-            _, _, _, _, st_bf, _ = Q.tune_dslash(nr, inner)
+            st_bf = Q.tune_dslash(nr, inner)[4]
             solves.append({"N": n, "nrhs": nr, "inner": iname, "seconds": round(sec, 4),
                            "iterations": prm.iterations, "reliable_updates": prm.reliable_updates,
                            "inner_dslash": ("tensor_core_variant_%d" % -st_bf) if st_bf < 0 else "cuda_core",

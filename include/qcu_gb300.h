@@ -206,10 +206,19 @@ int qcuDslashSegments(const QcuHopSegment *segments, int count, int nColors, int
  * (registers per thread: 1 no cap, 2 = 128, 3 = 85, 4 = 112, 5 = 96,
  * 6 = 104), whether the packed FP32x2 arithmetic variant was chosen, and the
  * ring depth of the TMA-staged kernel (0: the register kernel was chosen;
- * -v: tensor-core variant v, see qcuDslashKernels), and whether the kernel
- * reads two-row SU(3) links (recon = 1). */
+ * -v: tensor-core variant v, see qcuDslashKernels), whether the kernel
+ * reads two-row SU(3) links (recon = 1), and whether its links are staged by
+ * TMA per x-row (linktma = 1).  Any output pointer may be NULL. */
 int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int *reg_cap, int *packed, int *stages,
-                  int *recon);
+                  int *recon, int *linktma);
+
+/* No counterpart in the reference.  The kernel shape that the last
+ * single-lattice dslash launched by the calling thread ran, after the dispatcher's fallbacks (a
+ * pinned or tuned shape whose kernel cannot take the arguments runs the
+ * register kernel): shape[0..5] = (RHS per thread, register-cap variant,
+ * packed, stages, recon, linktma) as in qcuDslashKernels; all zero before the
+ * thread's first dslash. */
+int qcuLastDslashShape(int *shape);
 
 /* No counterpart in the reference.  FMA throughput of the current GPU in
  * TFLOP/s (2 flop per FMA), precision QCU_DOUBLE_PRECISION or
@@ -217,17 +226,20 @@ int qcuTuneDslash(int nrhs, int precision, int *rhs_per_thread, int *block, int 
  * the FP64 dslash.  Synchronous; takes a few milliseconds. */
 int qcuMeasureFmaRate(int precision, double *tflops);
 
-/* The compiled dslash kernel shapes for (precision, nColors): *count 5-tuples
- * (RHS per thread, register-cap variant, packed, stages, recon) are
- * available; the first max_shapes are written to shapes[5 * i .. 5 * i + 4].
+/* The compiled dslash kernel shapes for (precision, nColors): *count 6-tuples
+ * (RHS per thread, register-cap variant, packed, stages, recon, linktma) are
+ * available; the first max_shapes are written to shapes[6 * i .. 6 * i + 5].
  * stages > 0 is the TMA-staged kernel with that many ring buffers, stages < 0
  * a tensor-core (tcgen05) kernel, BF16 only: -1 projected half-spinor
  * operands with direct loads, -2 / -3 the same with a TMA ring of that depth,
  * -4 / -5 / -6 the neighbour spinor block as the MMA operand (warp-specialised,
  * TMA and B rings of different depths; nrhs a multiple of 4); recon = 1 reads
  * SU(3) links as two rows and reconstructs the third (used only when the
- * loaded gauge is SU(3) to the precision's rounding).  Any shape can be
- * pinned with QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon"
+ * loaded gauge is SU(3) to the precision's rounding); linktma = 1 is the
+ * register kernel with one CTA per x-row whose links are staged by TMA into
+ * shared memory (used when X/2 x the complex size is a multiple of 16 bytes
+ * and X/2 x nrhs / R <= 512).  Any shape can be pinned with
+ * QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon,linktma"
  * (tensor = 1..6 for the tensor-core variants). */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 

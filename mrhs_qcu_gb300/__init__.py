@@ -74,7 +74,7 @@ ABI_SYMBOLS = ["initGridSize", "pushBackFermions", "startDslash", "loadQcuGauge"
 EXT_SYMBOLS = ["qcuGetLastError", "qcuGetLastErrorString", "qcuClearError", "qcuVersion", "qcuSetAntiperiodicT",
                "qcuSetStream", "qcuSynchronize", "qcuFieldBytes", "qcuPackFermions", "qcuUnpackFermions",
                "qcuLoadGaugeLex", "qcuLexToEo", "qcuEoToLex", "qcuDslashMRHS", "qcuDslashXpayMRHS",
-               "qcuTuneDslash", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
+               "qcuTuneDslash", "qcuLastDslashShape", "qcuDslashKernels", "qcuMeasureFmaRate", "qcuSolverParamDefaults", "qcuInvert", "qcuNorm2MRHS",
                "qcuNorm2MRHSNoAlloc", "qcuBlasMRHS", "qcuCheckWaitTimeout", "qcuDslashSegments", "qcuLoadClover", "qcuCloverMRHS",
                "qcuServerCreate", "qcuServerAddGauge", "qcuServerSubmit", "qcuServerWait", "qcuServerStats",
                "qcuServerDestroy"]
@@ -140,8 +140,9 @@ def lib() -> ctypes.CDLL:
         "qcuDslashMRHS": ([P, P, P, P, I, I, I, I], I),
         "qcuDslashXpayMRHS": ([P, P, P, P, P, P, I, I, I, I, D, D], I),
         "qcuTuneDslash": ([I, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I),
-                           ctypes.POINTER(I), ctypes.POINTER(I)], I),
+                           ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)], I),
         "qcuDslashKernels": ([I, I, ctypes.POINTER(I), I, ctypes.POINTER(I)], I),
+        "qcuLastDslashShape": ([ctypes.POINTER(I)], I),
         "qcuMeasureFmaRate": ([I, ctypes.POINTER(ctypes.c_double)], I),
         "qcuLoadClover": ([P], I),
         "qcuCloverMRHS": ([P, P, P, P, I, I, I, I], I),
@@ -351,24 +352,33 @@ def blas_mrhs(op: int, n_elements: int, nrhs: int, x, x_precision: int, y=None, 
 
 
 def tune_dslash(nrhs: int, precision: int):
-    """(R, block, reg_cap, packed, stages, recon) of the tuned kernel; stages
-    > 0: the TMA-staged kernel, -v: tensor-core variant v (1-3 projected
-    half-spinor operands, 4-6 the spinor block as the MMA operand); recon:
-    two-row SU(3) links."""
-    R, B, M, K, T, C = (ctypes.c_int() for _ in range(6))
+    """(R, block, reg_cap, packed, stages, recon, linktma) of the tuned
+    kernel; stages > 0: the TMA-staged kernel, -v: tensor-core variant v (1-3
+    projected half-spinor operands, 4-6 the spinor block as the MMA operand);
+    recon: two-row SU(3) links; linktma: links staged by TMA per x-row."""
+    R, B, M, K, T, C, X = (ctypes.c_int() for _ in range(7))
     _raise_if(lib().qcuTuneDslash(int(nrhs), int(precision), ctypes.byref(R), ctypes.byref(B), ctypes.byref(M),
-                                  ctypes.byref(K), ctypes.byref(T), ctypes.byref(C)))
-    return R.value, B.value, M.value, K.value, T.value, C.value
+                                  ctypes.byref(K), ctypes.byref(T), ctypes.byref(C), ctypes.byref(X)))
+    return R.value, B.value, M.value, K.value, T.value, C.value, X.value
+
+
+def last_dslash_shape():
+    """(R, reg_cap, packed, stages, recon, linktma) of the kernel this
+    thread's last dslash launched, after the dispatcher's fallbacks."""
+    arr = (ctypes.c_int * 6)()
+    _raise_if(lib().qcuLastDslashShape(arr))
+    return tuple(arr)
 
 
 def dslash_kernels(precision: int, n_colors: int = 3):
-    """Compiled dslash kernel shapes [(R, reg_cap, packed, stages, recon), ...];
-    stages > 0: the TMA-staged kernel, -v: tensor-core variant v (1-6); recon:
-    two-row SU(3) links."""
-    arr = (ctypes.c_int * (5 * 64))()
+    """Compiled dslash kernel shapes [(R, reg_cap, packed, stages, recon,
+    linktma), ...]; stages > 0: the TMA-staged kernel, -v: tensor-core variant
+    v (1-6); recon: two-row SU(3) links; linktma: links staged by TMA per
+    x-row."""
+    arr = (ctypes.c_int * (6 * 96))()
     cnt = ctypes.c_int()
-    _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 64, ctypes.byref(cnt)))
-    return [tuple(arr[5 * i:5 * i + 5]) for i in range(min(cnt.value, 64))]
+    _raise_if(lib().qcuDslashKernels(int(precision), int(n_colors), arr, 96, ctypes.byref(cnt)))
+    return [tuple(arr[6 * i:6 * i + 6]) for i in range(min(cnt.value, 96))]
 
 
 def load_clover(clover_ptr) -> None:

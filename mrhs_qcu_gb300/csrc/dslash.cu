@@ -17,8 +17,8 @@ std::mutex& registry_mutex() {
   static std::mutex m;
   return m;
 }
-int key(int prec, int N, int R, int minb, int pk, int rc) {
-  return ((((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk) * 2 + rc;
+int key(int prec, int N, int R, int minb, int pk, int rc, int lt = 0) {
+  return (((((prec * 16 + N) * 16 + R) * 8 + minb) * 2 + pk) * 2 + rc) * 2 + lt;
 }
 std::map<int, SegmentsLauncher>& seg_registry() {
   static std::map<int, SegmentsLauncher> r;
@@ -53,18 +53,22 @@ int segments_options(int prec, int N, int* out, int max) {
   return n;
 }
 
-void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn) {
+void register_dslash(int prec, int N, int R, int minb, int pk, int rc, int lt, DslashLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[key(prec, N, R, minb, pk, rc)] = fn;
+  registry()[key(prec, N, R, minb, pk, rc, lt)] = fn;
+}
+
+void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn) {
+  register_dslash(prec, N, R, minb, pk, rc, 0, fn);
 }
 
 void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn) {
   register_dslash(prec, N, R, minb, pk, 0, fn);
 }
 
-DslashLauncher find_dslash(int prec, int N, int R, int minb, int pk, int rc) {
+DslashLauncher find_dslash(int prec, int N, int R, int minb, int pk, int rc, int lt) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find(key(prec, N, R, minb, pk, rc));
+  auto it = registry().find(key(prec, N, R, minb, pk, rc, lt));
   return it == registry().end() ? nullptr : it->second;
 }
 
@@ -75,10 +79,10 @@ int dslash_r_options(int prec, int N, int* out, int max) {
   return n;
 }
 
-int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc) {
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc, int lt) {
   int n = 0;
   for (int m = 1; m <= 7 && n < max; m++)
-    if (find_dslash(prec, N, R, m, pk, rc)) out[n++] = m;
+    if (find_dslash(prec, N, R, m, pk, rc, lt)) out[n++] = m;
   return n;
 }
 
@@ -103,6 +107,17 @@ bool tc_runs(const DslashArgs& A, int prec, int N, int variant) {
          tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);
 }
 
+namespace {
+DslashConfig no_launch() {
+  DslashConfig c;
+  c.R = c.block = c.minb = 0;
+  return c;
+}
+thread_local DslashConfig g_last_launched = no_launch();  // the shape last launched on this thread
+}
+
+DslashConfig last_launched_dslash() { return g_last_launched; }
+
 void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
   DslashConfig cfg = cfg_in;
   if (cfg.tc && tc_runs(A, prec, N, cfg.tc)) {
@@ -111,6 +126,8 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
     B.bf = (float)A.b;
     find_tc(prec, N, cfg.tc)(B, st);
     QCU_CHECK_CUDA(cudaGetLastError());
+    g_last_launched = DslashConfig{};
+    g_last_launched.R = 1, g_last_launched.tc = cfg.tc;
     return;
   }
   if (cfg.tc) {  // arguments the tensor-core kernel cannot take: register kernel
@@ -132,6 +149,8 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
       B.bf = (float)A.b;
       find_tma(prec, N, cfg.R, cfg.tma)(B, cfg.rcta, st);
       QCU_CHECK_CUDA(cudaGetLastError());
+      g_last_launched = DslashConfig{};
+      g_last_launched.R = cfg.R, g_last_launched.tma = cfg.tma, g_last_launched.rcta = cfg.rcta;
       return;
     }
     // arguments the staged kernel cannot take (e.g. a misaligned caller buffer): register kernel
@@ -144,12 +163,16 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
         break;
       }
   }
-  if (cfg.rc && (!A.gauge12 || !find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 1))) {
+  if (cfg.rc && (!A.gauge12 || !find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 1, cfg.lt))) {
     // no two-row gauge for this field (not SU(3) to rounding): the full links
     cfg.rc = 0;
-    if (!find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 0)) cfg.minb = 1, cfg.pk = 0;
+    if (!find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, 0, cfg.lt)) cfg.minb = 1, cfg.pk = 0, cfg.lt = 0;
   }
-  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, cfg.rc);
+  if (cfg.lt && !tmalink_runs(A, cfg.R, prec_complex_bytes(prec), cfg.rc ? (N - 1) * N : N * N)) {
+    cfg.lt = 0;  // arguments the link-staged kernel cannot take: the register kernel of the same shape
+    if (!find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, cfg.rc)) cfg.minb = 1, cfg.pk = 0;
+  }
+  DslashLauncher fn = find_dslash(prec, N, cfg.R, cfg.minb, cfg.pk, cfg.rc, cfg.lt);
   QCU_REQUIRE(fn != nullptr, QCU_ERR_UNSUPPORTED,
               std::string("no dslash kernel for precision ") + prec_name(prec) + ", N=" + std::to_string(N) +
                   ", R=" + std::to_string(cfg.R) + ", minb=" + std::to_string(cfg.minb) +
@@ -170,6 +193,8 @@ void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg
   B.bf = (float)A.b;
   fn(B, cfg.block, st);
   QCU_CHECK_CUDA(cudaGetLastError());
+  cfg.tma = cfg.rcta = cfg.tc = 0;
+  g_last_launched = cfg;
 }
 
 int launch_dslash_segments(const std::vector<DslashArgs>& all, int prec, int N, const DslashConfig& cfg_in,

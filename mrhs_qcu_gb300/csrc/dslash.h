@@ -18,14 +18,21 @@ using DslashLauncher = void (*)(const DslashArgs&, int block, cudaStream_t);
 // register-cap variant of the kernel (RegCap in dslash_kernel.cuh)
 // pk selects the packed FP32x2 arithmetic variant
 // rc selects the SU(3) variant that reads two-row links and reconstructs the third
-DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0, int rc = 0);
+// lt selects the register kernel with its links staged by TMA into shared memory (dslash_tmalink.cuh)
+DslashLauncher find_dslash(int prec, int N, int R, int minb = 1, int pk = 0, int rc = 0, int lt = 0);
 void register_dslash(int prec, int N, int R, int minb, int pk, DslashLauncher fn);
 void register_dslash(int prec, int N, int R, int minb, int pk, int rc, DslashLauncher fn);
+void register_dslash(int prec, int N, int R, int minb, int pk, int rc, int lt, DslashLauncher fn);
 
 // RHS-per-thread values compiled for (prec, N), largest first
 int dslash_r_options(int prec, int N, int* out, int max);
-// register-cap variants compiled for (prec, N, R, pk), ascending
-int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc = 0);
+// The link-staged kernel: dynamic shared memory for NN stored components per
+// link, hx sites per row and ebytes per complex; whether it can run A with R
+// RHS per thread (alignment, box, block and shared-memory limits).
+size_t tmalink_smem_bytes(int nn, int hx, int ebytes);
+bool tmalink_runs(const DslashArgs& A, int R, int ebytes, int nn);
+// register-cap variants compiled for (prec, N, R, pk, rc, lt), ascending
+int dslash_minb_options(int prec, int N, int R, int pk, int* out, int max, int rc = 0, int lt = 0);
 
 struct DslashConfig {
   int R = 1;
@@ -36,7 +43,12 @@ struct DslashConfig {
   int rcta = 0;  // its RHS per tile (0: the largest that fits)
   int tc = 0;    // tensor-core kernel (dslash_tc.cuh): 1 direct loads, 2 / 3 TMA ring of that depth
   int rc = 0;    // 1: SU(3) two-row links with the third row reconstructed (register kernel)
+  int lt = 0;    // 1: the register kernel with its links staged by TMA (one CTA per x-row)
 };
+
+// The shape launch_dslash last launched on the calling thread (after its
+// fallbacks: a pinned shape the arguments rule out runs another kernel).
+DslashConfig last_launched_dslash();
 
 // whether the staged kernel of cfg can run these arguments
 bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg);

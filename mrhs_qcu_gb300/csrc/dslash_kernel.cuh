@@ -160,16 +160,26 @@ __device__ __forceinline__ void load_norms(const float* p, float (&nrm)[R]) {
   }
 }
 
+// One link component: a read-only global load, or a shared-memory load where
+// the links were staged there (SMEM).
+template <typename E, bool SMEM>
+__device__ __forceinline__ E ld_link(const char* p) {
+  if constexpr (SMEM)
+    return *reinterpret_cast<const E*>(p);
+  else
+    return __ldg(reinterpret_cast<const E*>(p));
+}
+
 // SU(3) link from its first two rows: row 2 = conj(row 0 x row 1), each real
 // part one multiply and three FMAs (the reference's two-row gauge read,
 // include/kernels/storageLoadStore/loadAndStore.cuh:17-27, completed in
 // registers).  Loads the six stored components at lbase + k * ls_bytes.
-template <typename S, typename T>
+template <typename S, typename T, bool SMEM = false>
 __device__ __forceinline__ void load_su3_two_row(const char* lbase, uint32_t ls_bytes, C2<T> (&u)[3][3]) {
   using E = typename S::elem;
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    const auto v = S::to_c(__ldg(reinterpret_cast<const E*>(lbase)));
+    const auto v = S::to_c(ld_link<E, SMEM>(lbase));
     u[k / 3][k % 3].x = (T)v.x;
     u[k / 3][k % 3].y = (T)v.y;
     lbase += ls_bytes;
@@ -335,11 +345,12 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 // Each lane performs exactly the FMA sequence of hop() for its RHS, so the
 // results are bit-identical to it.  The 4N spinor components are loaded in
 // order with a running pointer (64-bit adds instead of wide multiply-adds).
-template <int P, int N, int R, int MU, bool FWD, bool RC>
+// The link's components lie at lbase + k * ls_bytes (global memory, or shared
+// memory when SMEM).
+template <int P, int N, int R, int MU, bool FWD, bool RC, bool SMEM = false>
 __device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4][N][R / 2], const DslashArgs& A,
-                                       const typename Store<P>::elem* __restrict__ in,
-                                       const typename Store<P>::elem* __restrict__ gauge, uint32_t link_off,
-                                       uint32_t nb, uint32_t rhs0, float bc, float f) {
+                                       const typename Store<P>::elem* __restrict__ in, const char* lbase,
+                                       uint32_t ls_bytes, uint32_t nb, uint32_t rhs0, float bc, float f) {
   using S = Store<P>;
   using E = typename S::elem;
   static_assert(R % 2 == 0, "packed arithmetic pairs the RHS of a thread");
@@ -406,12 +417,10 @@ __device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4
       }
     }
 
-  const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
-  const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);
   C2<float> ul[RC ? 3 : 1][RC ? 3 : 1];
   if constexpr (RC) {
     static_assert(N == 3, "link reconstruction is SU(3) only");
-    load_su3_two_row<S, float>(lbase, ls_bytes, ul);
+    load_su3_two_row<S, float, SMEM>(lbase, ls_bytes, ul);
   }
   const float klo0 = s * (float)gsign(MU, u0p), klo1 = s * (float)gsign(MU, u1p);
 #pragma unroll
@@ -426,7 +435,7 @@ __device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4
         uim = uc.y;
       } else {
         const uint32_t comp_l = FWD ? (a * N + b) : (b * N + a);
-        const float2 uc = S::to_c(__ldg(reinterpret_cast<const E*>(lbase + (uint64_t)comp_l * ls_bytes)));
+        const float2 uc = S::to_c(ld_link<E, SMEM>(lbase + (uint64_t)comp_l * ls_bytes));
         ur = uc.x;
         uim = uc.y;
       }
@@ -528,7 +537,8 @@ __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK
                                        uint32_t nb, uint32_t rhs0, typename Store<P>::real bc,
                                        typename Store<P>::real f) {
   if constexpr (PK)
-    hop_pk<P, N, R, MU, FWD, RC>(acc.re, acc.im, A, in, gauge, link_off, nb, rhs0, bc, f);
+    hop_pk<P, N, R, MU, FWD, RC>(acc.re, acc.im, A, in, reinterpret_cast<const char*>(gauge + link_off),
+                                 (uint32_t)A.geo.vh * (uint32_t)sizeof(typename Store<P>::elem), nb, rhs0, bc, f);
   else
     hop<P, N, R, MU, FWD, RC>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
 }

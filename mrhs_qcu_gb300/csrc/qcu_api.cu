@@ -631,31 +631,39 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     QCU_REQUIRE(count != nullptr && (shapes != nullptr || max_shapes == 0) && max_shapes >= 0,
                 QCU_ERR_INVALID_ARGUMENT, "qcuDslashKernels: bad output arrays");
     int n = 0;
-    auto put = [&](int R, int m, int pk, int st, int rc) {
+    auto put = [&](int R, int m, int pk, int st, int rc, int lt) {
       if (n < max_shapes) {
-        shapes[5 * n] = R;
-        shapes[5 * n + 1] = m;
-        shapes[5 * n + 2] = pk;
-        shapes[5 * n + 3] = st;
-        shapes[5 * n + 4] = rc;
+        int* o = shapes + 6 * n;
+        o[0] = R, o[1] = m, o[2] = pk, o[3] = st, o[4] = rc, o[5] = lt;
       }
       n++;
     };
     for (int R = 1; R <= 8; R++)
-      for (int v = 0; v < 3; v++)
-        for (int m = 1; m <= 7; m++)
-          if (qcu::find_dslash(precision, nColors, R, m, v == 1, v == 2)) put(R, m, v == 1, 0, v == 2);
+      for (int v = 0; v < 8; v++)  // packed x two-row links x links staged by TMA
+        for (int m = 1; m <= 7; m++) {
+          const int pk = v & 1, rc = (v >> 1) & 1, lt = v >> 2;
+          if (qcu::find_dslash(precision, nColors, R, m, pk, rc, lt)) put(R, m, pk, 0, rc, lt);
+        }
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
-    for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0);
+    for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0, 0);
     for (int v = 1; v <= 6; v++)
-      if (qcu::find_tc(precision, nColors, v)) put(1, 0, 0, -v, 0);
+      if (qcu::find_tc(precision, nColors, v)) put(1, 0, 0, -v, 0, 0);
     *count = n;
   });
 }
 
+int qcuLastDslashShape(int* shape) {
+  return guarded_unlocked([&] {
+    QCU_REQUIRE(shape != nullptr, QCU_ERR_INVALID_ARGUMENT, "qcuLastDslashShape: null output");
+    const qcu::DslashConfig c = qcu::last_launched_dslash();
+    shape[0] = c.R, shape[1] = c.minb, shape[2] = c.pk, shape[3] = c.tc ? -c.tc : c.tma, shape[4] = c.rc,
+    shape[5] = c.lt;
+  });
+}
+
 int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int* min_blocks, int* packed,
-                  int* stages, int* recon) {
+                  int* stages, int* recon, int* linktma) {
   return guarded([&] {
     Session& s = session();
     QCU_REQUIRE(qcu::prec_valid(precision), QCU_ERR_INVALID_ARGUMENT, "bad precision");
@@ -693,6 +701,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     if (packed) *packed = c.pk;
     if (stages) *stages = c.tc ? -c.tc : c.tma;
     if (recon) *recon = c.rc;
+    if (linktma) *linktma = c.lt;
   });
 }
 

@@ -79,6 +79,7 @@ void Autotuner::load_file() {
     if (!(ls >> c.tma >> c.rcta)) c.tma = c.rcta = 0;
     if (!(ls >> c.tc)) c.tc = 0;
     if (!(ls >> c.rc)) c.rc = 0;
+    if (!(ls >> c.lt)) c.lt = 0;
     cache_[k] = c;
   }
 }
@@ -89,29 +90,32 @@ void Autotuner::save_file() {
   std::ofstream out(path);
   for (auto& kv : cache_)
     out << kv.first << " " << kv.second.R << " " << kv.second.block << " " << kv.second.minb << " " << kv.second.pk
-        << " " << kv.second.tma << " " << kv.second.rcta << " " << kv.second.tc << " " << kv.second.rc << "\n";
+        << " " << kv.second.tma << " " << kv.second.rcta << " " << kv.second.tc << " " << kv.second.rc << " "
+        << kv.second.lt << "\n";
 }
 
 DslashConfig Autotuner::lookup(int prec, int N, int nrhs, int vh, bool* found) {
   std::lock_guard<std::mutex> lk(m_);
-  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta[,tensor[,recon]]]]]]" pins the kernel
-  // shape (profiling, sweeps); stages > 0 selects the TMA-staged kernel, tensor = 1 the tensor-core
-  // kernel (the other fields are then ignored); recon = 1 the register kernel on two-row SU(3) links
+  // QCU_DSLASH_CONFIG="R,block[,reg_cap[,packed[,stages[,rcta[,tensor[,recon[,linktma]]]]]]]" pins the
+  // kernel shape (profiling, sweeps); stages > 0 selects the TMA-staged kernel, tensor = 1 the tensor-core
+  // kernel (the other fields are then ignored); recon = 1 the register kernel on two-row SU(3) links;
+  // linktma = 1 the register kernel with its links staged by TMA
   if (const char* f = getenv("QCU_DSLASH_CONFIG")) {
     DslashConfig c;
-    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc,
-                           &c.rc);
+    const int got = sscanf(f, "%d,%d,%d,%d,%d,%d,%d,%d,%d", &c.R, &c.block, &c.minb, &c.pk, &c.tma, &c.rcta, &c.tc,
+                           &c.rc, &c.lt);
     if (got < 8) c.rc = 0;
+    if (got < 9) c.lt = 0;
     const bool tensor = got >= 7 && c.tc >= 1 && find_tc(prec, N, c.tc);
     const bool staged = !tensor && got >= 5 && c.tma > 0 && c.R >= 1 && nrhs % c.R == 0 &&
                         find_tma(prec, N, c.R, c.tma);
     const bool plain = !tensor && got >= 2 && c.tma <= 0 && c.R >= 1 && nrhs % c.R == 0 &&
-                       find_dslash(prec, N, c.R, c.minb, c.pk, c.rc) && c.block >= 32 && c.block <= 256 &&
+                       find_dslash(prec, N, c.R, c.minb, c.pk, c.rc, c.lt) && c.block >= 32 && c.block <= 256 &&
                        c.block % 32 == 0;
     if (tensor || staged || plain) {
       if (!staged) c.tma = c.rcta = 0;
       if (!tensor) c.tc = 0;
-      if (!plain) c.rc = 0;
+      if (!plain) c.rc = c.lt = 0;
       *found = true;
       return c;
     }
@@ -160,19 +164,23 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   float best_ms = 1e30f;
   for (int i = 0; i < n; i++) {
     if (A.nrhs % opts[i]) continue;
-    for (int v = 0; v < 4; v++) {  // scalar / packed FP32x2 arithmetic x full / two-row links
-    const int pk = v & 1, rc = v >> 1;
+    // scalar / packed FP32x2 arithmetic x full / two-row links x links from L1 / staged by TMA
+    for (int v = 0; v < 8; v++) {
+    const int pk = v & 1, rc = (v >> 1) & 1, lt = v >> 2;
     if (rc && !A.gauge12) continue;
+    if (lt && !tmalink_runs(A, opts[i], prec_complex_bytes(prec), rc ? (N - 1) * N : N * N)) continue;
     int minbs[8];
-    const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8, rc);
+    const int nm = dslash_minb_options(prec, N, opts[i], pk, minbs, 8, rc, lt);
     for (int j = 0; j < nm; j++)
       for (int b : blocks) {
+        if (lt && b != blocks[0]) continue;  // the link-staged kernel's CTA is one x-row, whatever the block
         DslashConfig c;
         c.R = opts[i];
         c.block = b;
         c.minb = minbs[j];
         c.pk = pk;
         c.rc = rc;
+        c.lt = lt;
         launch_dslash(A, prec, N, c, st);  // warm-up
         QCU_CHECK_CUDA(cudaEventRecord(e0, st));
         const int reps = 3;

@@ -58,10 +58,11 @@ def test_colours_and_rhs_counts(cuda, qcu_lib, n, nrhs, prec):
 @pytest.mark.parametrize("L", [(4, 4, 4, 8), (12, 4, 6, 4)])
 def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     """Every compiled shape, pinned in turn, against the oracle: register
-    kernels (R, register cap, packed, two-row links), TMA-staged kernels (R,
-    stages) and the tensor-core kernel (BF16, N >= 4).  The packed FP32x2
-    kernels and the staged kernels are bit-identical to the scalar register
-    kernel of the same R and link form (they perform its FMA sequence); the
+    kernels (R, register cap, packed, two-row links, links staged by TMA),
+    TMA-staged kernels (R, stages) and the tensor-core kernel (BF16, N >= 4).
+    The packed FP32x2 kernels (links from L1 or from shared memory) and the
+    staged kernels are bit-identical to the scalar register kernel of the
+    same R and link form (they perform its FMA sequence); the
     tensor-core kernel rounds its operands to BF16 and meets the 16-bit
     tolerance."""
     Q = qcu_lib
@@ -73,22 +74,22 @@ def test_every_kernel_shape(cuda, qcu_lib, prec, n, L):
     assert shapes
     outs = {}
     try:
-        for i, (R, minb, pk, st, rc) in enumerate(shapes):
+        for i, (R, minb, pk, st, rc, lt) in enumerate(shapes):
             if nrhs % R or (n >= 6 and st != 0):  # N >= 6: staged and tensor-core kernels in their own tests
                 continue
-            os.environ["QCU_DSLASH_CONFIG"] = ("1,0,0,0,0,0,%d" % -st if st < 0 else "%d,%d,%d,%d,%d,0,0,%d" % (
-                R, (32, 64, 128, 256)[i % 4], minb, pk, st, rc))
+            os.environ["QCU_DSLASH_CONFIG"] = ("1,0,0,0,0,0,%d" % -st if st < 0 else "%d,%d,%d,%d,%d,0,0,%d,%d" % (
+                R, (32, 64, 128, 256)[i % 4], minb, pk, st, rc, lt))
             for d in (0, 1):  # (parity 0, dagger 0) and (parity 1, dagger 1)
                 got = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
-                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, rc, d)
-                outs[(R, minb, pk, st, rc, d)] = got
+                assert rel(got, ref[d]) < TOL[prec], (R, minb, pk, st, rc, lt, d)
+                outs[(R, minb, pk, st, rc, lt, d)] = got
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
-    for (R, minb, pk, st, rc, d), got in outs.items():
+    for (R, minb, pk, st, rc, lt, d), got in outs.items():
         if pk or st > 0:
-            for (r2, m2, p2, s2, rc2, d2), other in outs.items():
+            for (r2, m2, p2, s2, rc2, lt2, d2), other in outs.items():
                 if r2 == R and d2 == d and not p2 and not s2 and rc2 == rc:
-                    assert np.array_equal(got, other), (R, minb, pk, st, rc, m2, d)
+                    assert np.array_equal(got, other), (R, minb, pk, st, rc, lt, m2, d)
 
 
 @pytest.mark.parametrize("prec", [2, 1, 4])
@@ -109,6 +110,89 @@ def test_reconstructed_links_only_for_su3_fields(cuda, qcu_lib, prec):
             assert rel(got, O.dslash(psi, gauge, L, 1, 0, True)) < TOL[prec]
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
+
+
+def _pin(R, minb, pk, rc, lt, block=64):
+    return "%d,%d,%d,%d,0,0,0,%d,%d" % (R, block, minb, pk, rc, lt)
+
+
+@pytest.mark.parametrize("prec,rc,L,nrhs", [
+    (1, 1, (4, 4, 4, 8), 12), (1, 0, (4, 4, 4, 8), 2), (1, 1, (12, 4, 6, 4), 12), (1, 1, (16, 6, 4, 10), 64),
+    (1, 0, (8, 8, 8, 16), 24), (1, 1, (8, 8, 8, 16), 4), (4, 1, (8, 8, 8, 16), 12), (4, 1, (16, 6, 4, 10), 64)])
+def test_link_staged_kernel(cuda, qcu_lib, prec, rc, L, nrhs):
+    """The register kernel with its links staged by TMA into shared memory
+    (one CTA per x-row, eight boxes on eight mbarriers): against the oracle on
+    both parities, dagger flags and antiperiodic t, for rows of 2..8 sites,
+    1..32 RHS groups, full and two-row links, FP32 and BF16 storage; launched
+    (not a fallback) and bit-identical to the register kernel of the same R
+    and link form."""
+    Q = qcu_lib
+    g = S.random_gauge(L, 3, seed=600 + nrhs)
+    psi = S.random_fermions(L, 3, nrhs, seed=601 + nrhs)
+    minb = [s[1] for s in Q.dslash_kernels(prec, 3) if s[0] == 2 and s[2] == 1 and s[4] == rc and s[5] == 1][0]
+    plain = [s[1] for s in Q.dslash_kernels(prec, 3) if s[0] == 2 and s[2] == 1 and s[4] == rc and s[5] == 0]
+    try:
+        for d in (0, 1):
+            os.environ["QCU_DSLASH_CONFIG"] = _pin(2, minb, 1, rc, 1)
+            got = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
+            assert Q.last_dslash_shape()[4:] == (rc, 1), Q.last_dslash_shape()
+            assert rel(got, O.dslash(psi, g, L, d, d, True)) < TOL[prec], d
+            os.environ["QCU_DSLASH_CONFIG"] = _pin(2, plain[0], 1, rc, 0)
+            other = abi_dslash(cuda, Q, psi, g, L, d, d, prec, antiperiodic_t=True)
+            assert Q.last_dslash_shape()[5] == 0
+            assert np.array_equal(got, other), d
+    finally:
+        os.environ.pop("QCU_DSLASH_CONFIG", None)
+
+
+@pytest.mark.parametrize("L,prec", [((6, 4, 4, 4), 1), ((4, 4, 4, 8), 4), ((12, 4, 6, 4), 4)])
+def test_link_staged_kernel_falls_back(cuda, qcu_lib, L, prec):
+    """A row whose links are not a multiple of 16 bytes (X/2 = 3 sites in
+    FP32, 2 or 6 sites in BF16) cannot be a TMA box: the pinned link-staged
+    shape runs the register kernel, with the oracle's result."""
+    Q = qcu_lib
+    g = S.random_gauge(L, 3, seed=610)
+    psi = S.random_fermions(L, 3, 4, seed=611)
+    minb = [s[1] for s in Q.dslash_kernels(prec, 3) if s[0] == 2 and s[2] == 1 and s[4] == 1 and s[5] == 1][0]
+    os.environ["QCU_DSLASH_CONFIG"] = _pin(2, minb, 1, 1, 1)
+    try:
+        got = abi_dslash(cuda, Q, psi, g, L, 1, 0, prec, antiperiodic_t=True)
+        assert Q.last_dslash_shape()[5] == 0
+        assert rel(got, O.dslash(psi, g, L, 1, 0, True)) < TOL[prec]
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
+
+
+def test_link_staged_kernel_in_masked_solve(cuda, qcu_lib):
+    """The link-staged kernel as the FP32 inner dslash of the masked eo-CG
+    (8^3 x 16 SU(3), 6 RHS, one zero source, one 1e-3 smaller so that RHS
+    converge at different iterations): every RHS meets the tolerance by the
+    oracle's FP64 true residual and the zero source gives zero."""
+    torch, Q = cuda, qcu_lib
+    L, n, nr, kappa, tol = (8, 8, 8, 16), 3, 6, 0.12, 1e-9
+    g = S.random_gauge(L, n, seed=620)
+    b = S.random_fermions(L, n, nr, seed=621, parities=2)
+    b[1] *= 1e-3
+    b[4] = 0
+    minb = [s[1] for s in Q.dslash_kernels(1, 3) if s[0] == 2 and s[2] == 1 and s[4] == 1 and s[5] == 1][0]
+    os.environ["QCU_DSLASH_CONFIG"] = _pin(2, minb, 1, 1, 1)
+    try:
+        Q.initGridSize(L, n)
+        Q.set_antiperiodic_t(True)
+        dg = dev(torch, g)
+        Q.loadQcuGauge(dg.data_ptr())
+        db = [dev(torch, b[r]) for r in range(nr)]
+        dx = [torch.zeros_like(x) for x in db]
+        p = Q.solver_params(kappa=kappa, tol=tol, inner_precision=1, max_iter=5000)
+        Q.invert([x.data_ptr() for x in dx], [x.data_ptr() for x in db], p)
+    finally:
+        del os.environ["QCU_DSLASH_CONFIG"]
+    assert float(dx[4].abs().max()) == 0.0
+    for r in range(nr):
+        assert p.converged[r], r
+        if r != 4:
+            res = O.true_residual(dx[r].cpu().numpy(), b[r], g, L, kappa, antiperiodic_t=True)
+            assert res < 2 * tol, (r, res)
 
 
 @pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
