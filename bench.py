@@ -67,7 +67,7 @@ def bytes_per_site_rhs(prec: int, n: int, nrhs: int) -> float:
     amortised over the RHS) + one input and one output spinor (4N complex)
     + the per-(site, RHS) FP32 scale of FP16 storage, read and written
     (BF16 fields are unscaled)."""
-    c = {2: 16, 1: 8, 0: 4, 4: 4}[prec]
+    c = {2: 16, 1: 8, 0: 4, 4: 4, 5: 4}[prec]
     nn = 4 if prec == 0 else 0
     return 8 * n * n * c / nrhs + 2 * (4 * n * c + nn)
 
@@ -264,7 +264,7 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     L = tuple(int(v) for v in args.lattice.split(","))
     n, nrhs, prec = args.ncolors, args.nrhs, args.precision
-    pname = {0: "fp16", 1: "fp32", 2: "fp64", 4: "bf16"}[prec]
+    pname = {0: "fp16", 1: "fp32", 2: "fp64", 4: "bf16", 5: "bf16-site"}[prec]
     vh = S.half_volume(L)
     g_dev, psi_dev = make_inputs(torch, L, n, nrhs, seed_g=0, seed_p=1 + rank)
 
@@ -306,7 +306,10 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     bpu = bytes_per_site_rhs(prec, n, nrhs)
     achieved = bpu * units / (ms_local * 1e-3) / 1e9
-    kernel = (("wilson_tcs_kernel<N=%d,stages=%d> (tcgen05)" % (n, -stages - 2)) if stages <= -4 else
+    tcs_rings = {4: (4, 3), 5: (6, 3), 6: (3, 2)}  # (TMA stages, B buffers) of variants 4-6
+    kernel = (("wilson_tcs_kernel<N=%d,stages=%d,bbufs=%d> (tcgen05, %s)"
+               % ((n,) + tcs_rings[-stages] + ("site-major" if prec == 5 else "component-major",)))
+              if stages <= -4 else
               ("wilson_tc_kernel<%s,N=%d> (tcgen05)" % (pname, n)) if stages < 0 else
               ("wilson_tma_kernel<%s,N=%d,R=%d,stages=%d>" % (pname, n, R, stages)) if stages else
               ("wilson_tmalink_kernel<%s,N=%d,R=%d,reg_cap=%d,recon=%d> row CTA"
@@ -470,7 +473,7 @@ def run_gpu(args):
             "metric": METRIC,
             "value": value, "unit": "site*RHS/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
+            "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f16", "bf16": "bf16", "bf16-site": "bf16"}[pname], "data": "synthetic (seeded SU(3) links, Gaussian spinors)",
             "config": workload_config(L, n, nrhs, world, pname),
             "roofline": roof, "rel_err": rel_err, "clocks": clk.summary(), "gpu_launches": args.steps,
             "e2e": e2e, "cpu_baseline": cpu, "sweep": sweep, "fma_peaks": fma, "solve": solve, "serve": serve,
@@ -525,7 +528,7 @@ def headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev, che
     del dsts
     ref = O.dslash(psi_dev[:checked].cpu().numpy(), g_dev.cpu().numpy(), L, 0, 0, True)
     errs = [float(np.linalg.norm(got[r] - ref[r]) / np.linalg.norm(ref[r])) for r in range(checked)]
-    tol = {2: 1e-13, 1: 1e-6, 0: 5e-3, 4: 5e-3}[prec]
+    tol = {2: 1e-13, 1: 1e-6, 0: 5e-3, 4: 5e-3, 5: 5e-3}[prec]
     return {"max": max(errs), "per_rhs": errs, "rhs_checked": checked, "tolerance": tol,
             "within_tolerance": max(errs) < tol,
             "against": "FP64 OpenMP oracle on the host, same inputs (D_eo, antiperiodic t)"}
@@ -609,7 +612,9 @@ def colors_bench(torch, Q, peak, fma):
                                       (4, "bf16", "tensor_core_projected", "1,0,0,0,0,0,1"),
                                       (4, "bf16", "tensor_core_projected_tma", "1,0,0,0,0,0,2"),
                                       (4, "bf16", "tensor_core_spinor", "1,0,0,0,0,0,4"),
-                                      (4, "bf16", "tensor_core_spinor_deep", "1,0,0,0,0,0,5")):
+                                      (4, "bf16", "tensor_core_spinor_deep", "1,0,0,0,0,0,5"),
+                                      (5, "bf16-site", "tensor_core_spinor", "1,0,0,0,0,0,4"),
+                                      (5, "bf16-site", "tensor_core_spinor_deep", "1,0,0,0,0,0,5")):
             for nr in (16, 32, 64):
                 if pin:
                     os.environ["QCU_DSLASH_CONFIG"] = pin
@@ -636,8 +641,10 @@ def colors_bench(torch, Q, peak, fma):
         Q.initGridSize(L, n)
         Q.set_antiperiodic_t(True)
         Q.loadQcuGauge(g_dev.data_ptr())
-        # FP32 inner (CUDA-core dslash) and BF16 inner (the autotuner's dslash: tensor cores where they win)
-        for inner, iname in ((Q.QCU_SINGLE_PRECISION, "fp32"), (Q.QCU_BF16_PRECISION, "bf16")):
+        # FP32 inner (CUDA-core dslash), BF16 inner (the autotuner's dslash: tensor cores where they win)
+        # and site-major BF16 inner (the tensor-core dslash)
+        for inner, iname in ((Q.QCU_SINGLE_PRECISION, "fp32"), (Q.QCU_BF16_PRECISION, "bf16"),
+                             (Q.QCU_BF16_SITE_PRECISION, "bf16-site")):
             prm = Q.solver_params(kappa=0.11, tol=1e-8, inner_precision=inner,
                                   solver=Q.QCU_SOLVER_BICGSTAB, max_iter=5000)
             for phase in ("cold", "warm"):
@@ -657,8 +664,9 @@ def colors_bench(torch, Q, peak, fma):
         del g_dev, psi, b, x
         torch.cuda.empty_cache()
     return {"workload": "16^3x32 SU(N) dslash: FP32 storage on CUDA cores; BF16 storage on CUDA cores (FP32 "
-                        "arithmetic) and on the tensor cores (tcgen05, BF16 operands, FP32 accumulation); "
-                        "BiCGStab kappa 0.11, FP32 and BF16 inner, 16 RHS (one 1e-4 smaller, one zero) to 1e-8",
+                        "arithmetic) and on the tensor cores (tcgen05, BF16 operands, FP32 accumulation), "
+                        "component-major and site-major (bf16-site) fields; BiCGStab kappa 0.11, FP32, BF16 and "
+                        "site-major BF16 inner, 16 RHS (one 1e-4 smaller, one zero) to 1e-8",
             "dslash": rows, "bicgstab": solves}
 
 

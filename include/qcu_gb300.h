@@ -52,6 +52,13 @@ typedef enum QcuStatus_e {
 #define QCU_DOUBLE_PRECISION 2
 #endif
 #define QCU_BF16_PRECISION 4
+/* BF16 storage in the site-major layout: resident fields [Vh][4N][nrhs]
+ * (every other code is component-major, [4N][Vh][nrhs]).  The dslash on
+ * these fields is the tensor-core kernel, which copies one site's whole
+ * block as one contiguous operand tile: nrhs a multiple of 4, N = 2..8, no
+ * clover term.  Accepted by pack/unpack, qcuDslashMRHS / qcuDslashXpayMRHS,
+ * qcuTuneDslash, qcuDslashKernels and as a solver inner precision. */
+#define QCU_BF16_SITE_PRECISION 5
 
 /* caller fermion address modes for pack/unpack */
 #define QCU_SRC_EO_HALF 0 /* one parity [Vh][4][N] */

@@ -24,6 +24,7 @@ QCU_HALF_PRECISION = 0
 QCU_SINGLE_PRECISION = 1
 QCU_DOUBLE_PRECISION = 2
 QCU_BF16_PRECISION = 4
+QCU_BF16_SITE_PRECISION = 5  # BF16, site-major field layout (tensor-core dslash)
 EVEN_PARITY = 0
 ODD_PARITY = 1
 QCU_DAGGER_NO = 0

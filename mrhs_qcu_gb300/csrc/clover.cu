@@ -227,6 +227,7 @@ void clover_apply(int prec, int N, const DslashArgs& A, const void* clover, cuda
     case PREC_SINGLE: launch_clover_n<PREC_SINGLE>(N, A, clover, st); break;
     case PREC_HALF: launch_clover_n<PREC_HALF>(N, A, clover, st); break;
     case PREC_BF16: launch_clover_n<PREC_BF16>(N, A, clover, st); break;
+    case PREC_BF16S: throw Error(QCU_ERR_UNSUPPORTED, "clover: site-major BF16 fields are not supported");
     default: throw Error(QCU_ERR_UNSUPPORTED, "bad precision");
   }
 }

@@ -94,10 +94,12 @@ bool tma_runs(const DslashArgs& A, int prec, int N, const DslashConfig& cfg) {
   return tma_plan(prec, N, A.geo, A.nrhs, cfg.R, cfg.tma, cfg.rcta, &T, &threads, &smem);
 }
 
-bool tc_runs(const DslashArgs& A, int prec, int N, int variant) {
+bool tc_runs(const DslashArgs& A_in, int prec, int N, int variant) {
   TcDslashArgs T;
   size_t smem = 0;
   if (!find_tc(prec, N, variant)) return false;
+  DslashArgs A = A_in;
+  A.site_major = prec_site_major(prec) ? 1 : 0;
   if (variant >= 4) {
     TcsDslashArgs T4;
     CUtensorMap m;
@@ -118,8 +120,19 @@ thread_local DslashConfig g_last_launched = no_launch();  // the shape last laun
 
 DslashConfig last_launched_dslash() { return g_last_launched; }
 
-void launch_dslash(const DslashArgs& A, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
+void launch_dslash(const DslashArgs& A_in, int prec, int N, const DslashConfig& cfg_in, cudaStream_t st) {
   DslashConfig cfg = cfg_in;
+  DslashArgs A = A_in;
+  A.site_major = prec_site_major(prec) ? 1 : 0;
+  if (A.site_major && !(cfg.tc >= 4 && tc_runs(A, prec, N, cfg.tc))) {
+    // site-major fields have only the spinor-operand tensor-core kernels: the first that runs
+    cfg = DslashConfig{};
+    for (int v = 4; v <= 6 && !cfg.tc; v++)
+      if (tc_runs(A, prec, N, v)) cfg.tc = v;
+    QCU_REQUIRE(cfg.tc, QCU_ERR_UNSUPPORTED,
+                "site-major BF16 fields need the tensor-core dslash: nrhs a multiple of 4, N = 2..8, 16-byte "
+                "aligned fields");
+  }
   if (cfg.tc && tc_runs(A, prec, N, cfg.tc)) {
     DslashArgs B = A;
     B.af = (float)A.a;

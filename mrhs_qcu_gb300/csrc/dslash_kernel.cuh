@@ -47,6 +47,7 @@ struct DslashArgs {
   int dagger;            // 0: f = +1, 1: f = -1
   int antiperiodic_t;
   FastDiv div_groups;    // G = nrhs / R
+  int site_major = 0;    // spinor fields in the site-major layout (PREC_BF16S; set by launch_dslash)
 };
 
 namespace detail {

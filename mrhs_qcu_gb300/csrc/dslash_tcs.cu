@@ -1,15 +1,19 @@
 // Instances of the spinor-operand tensor-core dslash (dslash_tcs.cuh):
-// tensor-core variants 4 / 5 / 6 (ring depths in dslash_tc.h), BF16, N = 3..8.
+// tensor-core variants 4 / 5 / 6 (ring depths in dslash_tc.h), BF16 in either
+// layout, N = 3..8.
 #include "dslash_tc.h"
 
 namespace qcu {
 namespace {
 
+// the same launchers serve both BF16 layouts (the plan reads the layout)
 template <int N>
 void register_n() {
-  register_tc(PREC_BF16, N, 4, &launch_wilson_tcs<N, 4>);
-  register_tc(PREC_BF16, N, 5, &launch_wilson_tcs<N, 5>);
-  register_tc(PREC_BF16, N, 6, &launch_wilson_tcs<N, 6>);
+  for (int prec : {(int)PREC_BF16, (int)PREC_BF16S}) {
+    register_tc(prec, N, 4, &launch_wilson_tcs<N, 4>);
+    register_tc(prec, N, 5, &launch_wilson_tcs<N, 5>);
+    register_tc(prec, N, 6, &launch_wilson_tcs<N, 6>);
+  }
 }
 
 struct RegisterTcs {

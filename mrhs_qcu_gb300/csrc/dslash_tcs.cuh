@@ -59,6 +59,9 @@ struct TcsDslashArgs {
   int ntiles;  // vh * chunks
   int halves;  // A boxes of 32 RHS per tile: 1 (rt <= 32) or 2
   int* err;    // set to 1 when a wait times out
+  // complex-element strides of the output and xpay fields between components
+  // and between sites (component- or site-major layout)
+  uint32_t cstr, sstr;
 };
 
 namespace tcs {
@@ -184,7 +187,11 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, vo
 }  // namespace tcs
 
 // map_in: the input field as [site][spin 4][colour N][RHS] of 4-byte complex
-// BF16, box (32 RHS, 8 colours, 4 spins, 1 site), 128-byte swizzle.  The
+// BF16 (strides of either layout), box (32 RHS, 8 colours, 4 spins, 1 site),
+// 128-byte swizzle.  In the site-major layout a box is one contiguous 4 KB
+// run of the field; in the component-major one it gathers 32 rows of 128
+// bytes from arrays Vh x nrhs x 4 bytes apart, which the copy engine serves
+// at about half the rate when a hop's block is 8 KB.  The
 // links come from A.gauge_tc (BF16 row form, one 256-byte bulk copy per hop).
 template <int N, int NST, int NB>
 __global__ void __launch_bounds__(tcs::kThreads, 4)
@@ -390,7 +397,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     const uint32_t lq = (uint32_t)warp & 3u;
     const uint32_t m = lq * 32u + (uint32_t)lane;
     const uint32_t r = m >> 1, ri = m & 1u;
-    const uint32_t vh = A.geo.vh, nrhs = A.nrhs, cs = vh * nrhs;
+    const uint32_t cstr = T.cstr, sstr = T.sstr;
     const __nv_bfloat16* __restrict__ xin = static_cast<const __nv_bfloat16*>(A.x);
     __nv_bfloat16* __restrict__ out = static_cast<__nv_bfloat16*>(A.out);
     int it = 0;
@@ -421,7 +428,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           const float own = __uint_as_float(re_k[a]);
           float val = ca * (ri ? own + other : own - other);
           if (live) {
-            const uint32_t idx = 2u * ((uint32_t)(s * N + a) * cs + site * nrhs + rhs) + ri;
+            const uint32_t idx = 2u * ((uint32_t)(s * N + a) * cstr + site * sstr + rhs) + ri;
             if (xin) val = fmaf(A.bf, __bfloat162float(xin[idx]), val);
             // streaming store: the output is not re-read by this launch
             __stcs(reinterpret_cast<unsigned short*>(out) + idx, __bfloat16_as_ushort(__float2bfloat16_rn(val)));

@@ -123,10 +123,12 @@ void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int n
   encode(m, ptr, dims, strides, box);
 }
 
-bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N) {
-  const cuuint64_t cs = (cuuint64_t)vh * nrhs * 4;  // component stride, bytes
+bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major) {
+  // byte strides of colour, spin and site
+  const cuuint64_t cs = site_major ? (cuuint64_t)nrhs * 4 : (cuuint64_t)vh * nrhs * 4;
+  const cuuint64_t ss = site_major ? (cuuint64_t)4 * N * nrhs * 4 : (cuuint64_t)nrhs * 4;
   const cuuint64_t dims[4] = {(cuuint64_t)nrhs, (cuuint64_t)N, 4, (cuuint64_t)vh};
-  const cuuint64_t strides[3] = {cs, (cuuint64_t)N * cs, (cuuint64_t)nrhs * 4};
+  const cuuint64_t strides[3] = {cs, (cuuint64_t)N * cs, ss};
   const cuuint32_t box[4] = {32, 8, 4, 1};
   const cuuint32_t es[4] = {1, 1, 1, 1};
   return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void*>(ptr), dims, strides, box, es,

@@ -28,9 +28,10 @@ void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int n
 // 16-bit storage scales [Vh][nrhs] float with box {rcta, hx}
 void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rcta, int hx);
 // the MRHS field of a tensor-core operand: [site][spin 4][colour N][RHS] of
-// 4-byte complex BF16, box (32 RHS, 8 colours, 4 spins, 1 site), 128-byte
-// swizzle, colours N..7 zero-filled; false when the driver rejects the map
-bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N);
+// 4-byte complex BF16 in the component- or site-major layout, box (32 RHS,
+// 8 colours, 4 spins, 1 site), 128-byte swizzle, colours N..7 zero-filled;
+// false when the driver rejects the map
+bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major);
 
 // Tile plan for (precision, N, geometry, nrhs, R, stages); rcta = 0 picks the
 // largest RHS chunk that fits.  False when the staged kernel cannot run these

@@ -50,9 +50,9 @@ __global__ void pack_fermions_kernel(PtrArray src, int mode, int parity, void* d
   double2 v[4 * N];
 #pragma unroll
   for (int c = 0; c < 4 * N; c++) v[c] = __ldg(s + c);
-  // component-major MRHS field: component c at (c * Vh + site) * nrhs + r
-  const int64_t cs = (int64_t)g.vh * nrhs;
-  E* d = static_cast<E*>(dst) + (int64_t)site * nrhs + r;
+  // component c at site * ss + c * cs + r (component- or site-major, by P)
+  const int64_t cs = field_comp_stride(P, g.vh, 4 * N, nrhs), ss = field_site_stride(P, g.vh, 4 * N, nrhs);
+  E* d = static_cast<E*>(dst) + (int64_t)site * ss + r;
   if constexpr (S::has_norm) {
     double m = 0.0;
 #pragma unroll
@@ -82,8 +82,8 @@ __global__ void unpack_fermions_kernel(PtrArray dstp, int mode, int parity, cons
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
   if ((int)site >= g.vh || dstp.p[r] == nullptr) return;  // a null pointer skips RHS r
-  const int64_t cs = (int64_t)g.vh * nrhs;
-  const E* s = static_cast<const E*>(src) + (int64_t)site * nrhs + r;
+  const int64_t cs = field_comp_stride(P, g.vh, 4 * N, nrhs), ss = field_site_stride(P, g.vh, 4 * N, nrhs);
+  const E* s = static_cast<const E*>(src) + (int64_t)site * ss + r;
   double2* d = static_cast<double2*>(const_cast<void*>(dstp.p[r])) + src_site(mode, site, parity, g) * (4 * N);
   double scale = 1.0;
   if constexpr (S::has_norm) scale = (double)src_norm[(int64_t)site * nrhs + r];
@@ -136,7 +136,7 @@ __global__ void unpack_gauge_kernel(const double2* __restrict__ src, double2* ds
   for (int k = 0; k < nn; k++) d[k] = s[(int64_t)k * vh];
 }
 
-// convert an MRHS field between storage precisions (same layout)
+// convert an MRHS field between storage precisions (and layouts)
 template <int PI, int PO>
 __global__ void convert_field_kernel(const void* src, const float* src_norm, void* dst, float* dst_norm,
                                      int64_t vh, int ncomp, int nrhs, FastDiv div_nrhs, const int* mask) {
@@ -146,23 +146,23 @@ __global__ void convert_field_kernel(const void* src, const float* src_norm, voi
   uint32_t site, r;
   div_nrhs.divmod(gid, site, r);
   if ((int64_t)site >= vh || (mask && !mask[r])) return;  // masked RHS keep their values
-  // component-major: component c at (c * vh + site) * nrhs + r
-  const int64_t cs = vh * nrhs;
-  const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * nrhs + r;
-  auto* d = static_cast<typename SO::elem*>(dst) + (int64_t)site * nrhs + r;
+  // component c at site * ss + c * cs + r, strides by each side's layout
+  const int64_t csi = field_comp_stride(PI, vh, ncomp, nrhs), csd = field_comp_stride(PO, vh, ncomp, nrhs);
+  const auto* s = static_cast<const typename SI::elem*>(src) + (int64_t)site * field_site_stride(PI, vh, ncomp, nrhs) + r;
+  auto* d = static_cast<typename SO::elem*>(dst) + (int64_t)site * field_site_stride(PO, vh, ncomp, nrhs) + r;
   double si = 1.0;
   if constexpr (SI::has_norm) si = (double)src_norm[(int64_t)site * nrhs + r];
   double m = 0.0;
   if constexpr (SO::has_norm) {
     for (int c = 0; c < ncomp; c++) {
-      auto v = SI::to_c(s[c * cs]);
+      auto v = SI::to_c(s[c * csi]);
       m = fmax(m, fmax(fabs((double)v.x * si), fabs((double)v.y * si)));
     }
     dst_norm[(int64_t)site * nrhs + r] = (float)m;
   }
   const double inv = SO::has_norm ? (m > 0.0 ? 1.0 / (double)(float)m : 0.0) : 1.0;
   for (int c = 0; c < ncomp; c++) {
-    auto v = SI::to_c(s[c * cs]);
+    auto v = SI::to_c(s[c * csi]);
     const double re = (double)v.x * si * inv, im = (double)v.y * si * inv;
     typename SO::elem e;
     if constexpr (PO == PREC_DOUBLE) {
@@ -172,7 +172,7 @@ __global__ void convert_field_kernel(const void* src, const float* src_norm, voi
     } else {
       e = SO::from_c(make_float2((float)re, (float)im));
     }
-    d[c * cs] = e;
+    d[c * csd] = e;
   }
 }
 
@@ -269,6 +269,7 @@ void pack_n(int prec, const PtrArray& src, int mode, int parity, void* dst, floa
     case PREC_SINGLE: pack_fermions_kernel<PREC_SINGLE, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
     case PREC_HALF: pack_fermions_kernel<PREC_HALF, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
     case PREC_BF16: pack_fermions_kernel<PREC_BF16, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
+    case PREC_BF16S: pack_fermions_kernel<PREC_BF16S, N><<<grid, block, 0, st>>>(src, mode, parity, dst, dst_norm, g, nrhs, dn); break;
   }
 }
 
@@ -284,6 +285,7 @@ void unpack_n(int prec, const PtrArray& dst, int mode, int parity, const void* s
     case PREC_SINGLE: unpack_fermions_kernel<PREC_SINGLE, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
     case PREC_HALF: unpack_fermions_kernel<PREC_HALF, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
     case PREC_BF16: unpack_fermions_kernel<PREC_BF16, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
+    case PREC_BF16S: unpack_fermions_kernel<PREC_BF16S, N><<<grid, block, 0, st>>>(dst, mode, parity, src, src_norm, g, nrhs, dn); break;
   }
 }
 
@@ -372,6 +374,13 @@ void convert_field(int prec_in, const void* src, const float* src_norm, int prec
   QCU_CONV(PREC_SINGLE, PREC_SINGLE)
   QCU_CONV(PREC_HALF, PREC_HALF)
   QCU_CONV(PREC_BF16, PREC_BF16)
+  QCU_CONV(PREC_DOUBLE, PREC_BF16S)
+  QCU_CONV(PREC_BF16S, PREC_DOUBLE)
+  QCU_CONV(PREC_SINGLE, PREC_BF16S)
+  QCU_CONV(PREC_BF16S, PREC_SINGLE)
+  QCU_CONV(PREC_BF16, PREC_BF16S)
+  QCU_CONV(PREC_BF16S, PREC_BF16)
+  QCU_CONV(PREC_BF16S, PREC_BF16S)
 #undef QCU_CONV
   throw Error(QCU_ERR_UNSUPPORTED, "unsupported precision conversion");
 }

@@ -674,7 +674,7 @@ int qcuTuneDslash(int nrhs, int precision, int* rhs_per_thread, int* block, int*
     qcu::DslashArgs A;
     A.gauge = s.gauge(precision);
     A.gauge12 = s.gauge12(precision);
-    if (precision == qcu::PREC_BF16 && nrhs % 4 == 0) A.gauge_tc = s.gauge_tc();
+    if (qcu::prec_bf16(precision) && nrhs % 4 == 0) A.gauge_tc = s.gauge_tc();
     A.in = fi.data;
     A.in_norm = fi.norm;
     A.out = fo.data;

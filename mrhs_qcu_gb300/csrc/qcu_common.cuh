@@ -23,11 +23,30 @@
 namespace qcu {
 
 // precision codes: the reference's QCU_PRECISION values (include/qcu_enum.h:4
-// of the reference) plus BF16 as an extension
-enum Prec : int { PREC_HALF = 0, PREC_SINGLE = 1, PREC_DOUBLE = 2, PREC_BF16 = 4 };
+// of the reference) plus BF16 as an extension, and BF16 in the site-major
+// layout (below) as a storage code of its own
+enum Prec : int { PREC_HALF = 0, PREC_SINGLE = 1, PREC_DOUBLE = 2, PREC_BF16 = 4, PREC_BF16S = 5 };
 
-inline bool prec_valid(int p) { return p == PREC_HALF || p == PREC_SINGLE || p == PREC_DOUBLE || p == PREC_BF16; }
-inline bool prec_is16(int p) { return p == PREC_HALF || p == PREC_BF16; }
+inline bool prec_valid(int p) {
+  return p == PREC_HALF || p == PREC_SINGLE || p == PREC_DOUBLE || p == PREC_BF16 || p == PREC_BF16S;
+}
+inline bool prec_is16(int p) { return p == PREC_HALF || p == PREC_BF16 || p == PREC_BF16S; }
+// BF16 storage of either layout
+inline bool prec_bf16(int p) { return p == PREC_BF16 || p == PREC_BF16S; }
+// Field layouts.  Component-major (every code but PREC_BF16S): component c of
+// site s, RHS r at (c * Vh + s) * nrhs + r.  Site-major (PREC_BF16S): at
+// (s * 4N + c) * nrhs + r, so one site's block of all components and RHS is
+// one contiguous run (the tensor-core kernel copies it as one operand tile).
+// Both keep the RHS innermost, so elementwise and per-RHS operations are
+// layout-blind.
+__host__ __device__ constexpr bool prec_site_major(int p) { return p == PREC_BF16S; }
+// element strides (in complexes) between components and between sites
+__host__ __device__ inline int64_t field_comp_stride(int p, int64_t vh, int ncomp, int nrhs) {
+  return prec_site_major(p) ? (int64_t)nrhs : vh * nrhs;
+}
+__host__ __device__ inline int64_t field_site_stride(int p, int64_t vh, int ncomp, int nrhs) {
+  return prec_site_major(p) ? (int64_t)ncomp * nrhs : (int64_t)nrhs + 0 * vh;
+}
 // FP16 fields carry a per-(site, RHS) FP32 scale; BF16 has the FP32 exponent
 // range, so its fields are stored unscaled
 inline bool prec_has_norm(int p) { return p == PREC_HALF; }
@@ -38,6 +57,7 @@ inline const char* prec_name(int p) {
     case PREC_SINGLE: return "fp32";
     case PREC_DOUBLE: return "fp64";
     case PREC_BF16: return "bf16";
+    case PREC_BF16S: return "bf16-site";
   }
   return "?";
 }
@@ -168,6 +188,8 @@ template <> struct Store<PREC_BF16> {
   __device__ __forceinline__ static float2 to_c(__nv_bfloat162 v) { return __bfloat1622float2(v); }
   __device__ __forceinline__ static __nv_bfloat162 from_c(float2 v) { return __float22bfloat162_rn(v); }
 };
+// site-major BF16: the same element, another layout
+template <> struct Store<PREC_BF16S> : Store<PREC_BF16> {};
 
 template <typename R> struct cplx;
 template <> struct cplx<float> { using t = float2; };

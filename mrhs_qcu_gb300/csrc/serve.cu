@@ -122,7 +122,7 @@ void Server::add_gauge(int gauge_id, const int L[4], int N, const void* gauge, i
   // memory: FP64 master gauge + the inner-precision copy + engine fields
   size_t gauge_bytes = (size_t)8 * s.geo.vh * N * N * (16 + prec_complex_bytes(p_->proto.inner_prec));
   // BF16 inner solves also keep the site-major link copy of the tensor-core dslash
-  if (p_->proto.inner_prec == PREC_BF16) gauge_bytes += tc_links_bytes(s.geo.vh);
+  if (prec_bf16(p_->proto.inner_prec)) gauge_bytes += tc_links_bytes(s.geo.vh);
   const size_t per_slot = SlotEngine::bytes_needed(s, 1, p_->proto.inner_prec);
   int cap = 0;
   {

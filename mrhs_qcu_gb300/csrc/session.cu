@@ -134,6 +134,10 @@ void Autotuner::store(int prec, int N, int nrhs, int vh, const DslashConfig& c) 
 
 DslashConfig Autotuner::heuristic(int prec, int N, int nrhs) {
   DslashConfig c;
+  if (prec_site_major(prec)) {  // only the spinor-operand tensor-core kernels take site-major fields
+    c.tc = 4;
+    return c;
+  }
   int opts[8];
   const int n = dslash_r_options(prec, N, opts, 8);
   int want = prec == PREC_DOUBLE ? 1 : (prec == PREC_SINGLE ? 2 : 4);
@@ -298,6 +302,7 @@ void Session::load_gauge(const void* caller_gauge, int lex) {
 const void* Session::gauge(int prec) {
   QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
   QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  if (prec == PREC_BF16S) prec = PREC_BF16;  // the field layout does not apply to links
   if (!gauge_valid_[prec]) {
     const int64_t count = (int64_t)8 * geo.vh * N * N;
     void* d = gauge_[prec].ensure((size_t)count * prec_complex_bytes(prec));
@@ -311,6 +316,7 @@ const void* Session::gauge(int prec) {
 const void* Session::gauge12(int prec) {
   QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
   QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  if (prec == PREC_BF16S) prec = PREC_BF16;
   if (N != 3) return nullptr;
   if (su3_dev_ < 0) {
     unsigned* scratch = static_cast<unsigned*>(su3_scratch_.ensure(16));
@@ -354,6 +360,7 @@ void Session::load_clover(const void* caller_clover) {
 const void* Session::clover(int prec, bool inverse) {
   QCU_REQUIRE(clover_loaded_, QCU_ERR_NO_OPERATOR, "no clover field loaded");
   QCU_REQUIRE(prec_valid(prec), QCU_ERR_INVALID_ARGUMENT, "bad precision");
+  QCU_REQUIRE(!prec_site_major(prec), QCU_ERR_UNSUPPORTED, "clover: site-major BF16 fields are not supported");
   DeviceBuffer* buf = inverse ? cloverinv_ : clover_;
   bool* valid = inverse ? cloverinv_valid_ : clover_valid_;
   if (!valid[prec]) {
@@ -412,7 +419,7 @@ void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagg
   A.gauge = gauge(in.prec);
   A.gauge12 = gauge12(in.prec);
   // BF16 RHS counts the spinor-operand tensor-core kernel takes
-  if (in.prec == PREC_BF16 && in.nrhs % 4 == 0) A.gauge_tc = gauge_tc();
+  if (prec_bf16(in.prec) && in.nrhs % 4 == 0) A.gauge_tc = gauge_tc();
   A.in = in.data;
   A.in_norm = in.norm;
   A.out = out.data;

@@ -236,6 +236,10 @@ SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const st
   QCU_REQUIRE(capacity >= 1 && capacity <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "slot capacity must be in 1..256");
   QCU_REQUIRE(q.solver == 0 || q.solver == 1, QCU_ERR_INVALID_ARGUMENT, "unknown solver");
   QCU_REQUIRE(prec_valid(q.inner_prec), QCU_ERR_INVALID_ARGUMENT, "bad inner precision");
+  QCU_REQUIRE(!(s.has_clover() && prec_site_major(q.inner_prec)), QCU_ERR_UNSUPPORTED,
+              "clover: site-major BF16 fields are not supported");
+  QCU_REQUIRE(!prec_site_major(q.inner_prec) || capacity % 4 == 0, QCU_ERR_UNSUPPORTED,
+              "site-major BF16 inner fields take the tensor-core dslash: the RHS count must be a multiple of 4");
   kp_ = q.inner_prec == PREC_DOUBLE ? PREC_DOUBLE : PREC_SINGLE;
   op_ = q.inner_prec;
   delta2_ = (q.inner_prec == PREC_DOUBLE) ? 0.0 : q.delta * q.delta;

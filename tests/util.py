@@ -28,4 +28,4 @@ def abi_dslash(torch, Q, psi, gauge, L, parity, dagger=0, prec=2, antiperiodic_t
     return np.stack([o.cpu().numpy() for o in outs])
 
 
-TOL = {2: 1e-13, 1: 1e-6, 0: 5e-3, 4: 5e-3}
+TOL = {2: 1e-13, 1: 1e-6, 0: 5e-3, 4: 5e-3, 5: 5e-3}
