@@ -9,8 +9,9 @@
   inner, each RHS checked by the oracle's FP64 true residual of the full
   Wilson system.
 * 16^3 x 32 SU(N), N = 4, 6, 8, nrhs 16 / 32 / 64: the CUDA-core kernels
-  (FP32, BF16) and the tensor-core kernels (BF16), and a masked BiCGStab to
-  1e-8 (one source 1e-4 smaller, one zero) checked RHS by RHS.
+  (FP32, BF16) and the tensor-core kernels (BF16, component- and site-major
+  fields), and a masked BiCGStab to 1e-8 (one source 1e-4 smaller, one
+  zero) checked RHS by RHS.
 
 Tolerances (relative L2): 1e-13 FP64, 1e-6 FP32, 5e-3 FP16/BF16; solves:
 the oracle's true residual at most 2x the requested tolerance."""
@@ -111,7 +112,8 @@ def test_solve_benchmark_workload(cuda, qcu_lib, inner):
 # (kernel name, storage precision, QCU_DSLASH_CONFIG pin or None for the autotuner)
 SUN_KERNELS = [("cuda_core_fp32", 1, None), ("cuda_core_bf16", 4, "2,64,1,0"),
                ("tensor_core_projected", 4, "1,0,0,0,0,0,1"), ("tensor_core_projected_tma", 4, "1,0,0,0,0,0,2"),
-               ("tensor_core_spinor", 4, "1,0,0,0,0,0,4"), ("tensor_core_spinor_deep", 4, "1,0,0,0,0,0,5")]
+               ("tensor_core_spinor", 4, "1,0,0,0,0,0,4"), ("tensor_core_spinor_deep", 4, "1,0,0,0,0,0,5"),
+               ("tensor_core_spinor_site_major", 5, "1,0,0,0,0,0,4")]
 
 
 @pytest.mark.parametrize("nrhs", [16, 32, 64])
