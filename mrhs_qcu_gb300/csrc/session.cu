@@ -132,6 +132,18 @@ void Autotuner::store(int prec, int N, int nrhs, int vh, const DslashConfig& c) 
   save_file();
 }
 
+bool Autotuner::layout_site_major(int N, int nrhs, int vh, bool* known) {
+  std::lock_guard<std::mutex> lk(m_);
+  auto it = layout_.find(key(PREC_BF16S, N, nrhs, vh));
+  *known = it != layout_.end();
+  return *known && it->second;
+}
+
+void Autotuner::store_layout(int N, int nrhs, int vh, bool site_major) {
+  std::lock_guard<std::mutex> lk(m_);
+  layout_[key(PREC_BF16S, N, nrhs, vh)] = site_major;
+}
+
 DslashConfig Autotuner::heuristic(int prec, int N, int nrhs) {
   DslashConfig c;
   if (prec_site_major(prec)) {  // only the spinor-operand tensor-core kernels take site-major fields
@@ -408,6 +420,48 @@ FieldView Session::alloc_field(const std::string& name, int prec, int nrhs) {
   f.data = ws.get(name, field_bytes(prec, nrhs));
   if (prec_has_norm(prec)) f.norm = static_cast<float*>(ws.get(name + ".norm", norm_bytes(prec, nrhs)));
   return f;
+}
+
+bool Session::prefer_site_major(FieldView a, FieldView b) {
+  const int nrhs = a.nrhs;
+  if (!prec_bf16(a.prec) || b.nrhs != nrhs || nrhs % 4 || !tuner.enabled()) return false;
+  bool known = false;
+  const bool cached = tuner.layout_site_major(N, nrhs, geo.vh, &known);
+  if (known) return cached;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  QCU_CHECK_CUDA(cudaStreamIsCapturing(stream(), &cs));
+  if (cs != cudaStreamCaptureStatusNone) return false;
+  // zero input (the bytes are the same in both layouts), then each layout's
+  // tuned dslash: one untimed application (tunes it), three timed
+  QCU_CHECK_CUDA(cudaMemsetAsync(a.data, 0, field_bytes(PREC_BF16, nrhs), stream()));
+  cudaEvent_t e0, e1;
+  QCU_CHECK_CUDA(cudaEventCreate(&e0));
+  QCU_CHECK_CUDA(cudaEventCreate(&e1));
+  float ms[2] = {0.f, 0.f};
+  bool ok = true;
+  for (int i = 0; i < 2 && ok; i++) {
+    a.prec = b.prec = i ? PREC_BF16S : PREC_BF16;
+    try {
+      hop(b, a, FieldView{}, 0, 0, 1.0, 0.0);
+      QCU_CHECK_CUDA(cudaEventRecord(e0, stream()));
+      for (int k = 0; k < 3; k++) hop(b, a, FieldView{}, 0, 0, 1.0, 0.0);
+      QCU_CHECK_CUDA(cudaEventRecord(e1, stream()));
+      QCU_CHECK_CUDA(cudaEventSynchronize(e1));
+      QCU_CHECK_CUDA(cudaEventElapsedTime(&ms[i], e0, e1));
+    } catch (const Error& e) {
+      if (e.code != QCU_ERR_UNSUPPORTED) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+      }
+      ok = false;  // the site-major kernel cannot take these arguments
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const bool site = ok && ms[1] < 0.95f * ms[0];
+  tuner.store_layout(N, nrhs, geo.vh, site);
+  return site;
 }
 
 void Session::hop(FieldView out, FieldView in, FieldView x, int parity, int dagger, double a, double b,

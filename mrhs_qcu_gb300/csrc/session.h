@@ -70,10 +70,14 @@ class Autotuner {
   // output buffers of A are overwritten
   DslashConfig tune(const DslashArgs& A, int prec, int N, cudaStream_t st);
   bool enabled() const;
+  // the BF16 field layout chosen for (N, nrhs, vh): *known = false if none yet
+  bool layout_site_major(int N, int nrhs, int vh, bool* known);
+  void store_layout(int N, int nrhs, int vh, bool site_major);
 
  private:
   std::mutex m_;
   std::map<std::string, DslashConfig> cache_;
+  std::map<std::string, bool> layout_;
   std::string key(int prec, int N, int nrhs, int vh) const;
   void load_file();
   void save_file();
@@ -181,6 +185,12 @@ class Session {
   // out = a * D in + b * x  (x.data may be null), on the library stream.
   // mask: per-RHS activity (masked RHS are left untouched); a_rhs_f / a_rhs_d:
   // per-RHS a (device arrays) for FP32 / FP64 arithmetic, replacing a.
+  // Whether BF16 operator fields of a.nrhs RHS are faster in the site-major
+  // layout (the tensor-core dslash on contiguous site blocks) than in the
+  // component-major one: timed once per (N, nrhs, volume) on a and b (two
+  // BF16 fields of this session, overwritten), then cached.  False where the
+  // site-major kernel cannot run, and during stream capture.
+  bool prefer_site_major(FieldView a, FieldView b);
   void hop(FieldView out, FieldView in, FieldView x, int parity, int dagger, double a, double b,
            const int* mask = nullptr, const float* a_rhs_f = nullptr, const double* a_rhs_d = nullptr);
 

@@ -236,7 +236,7 @@ SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const st
   QCU_REQUIRE(capacity >= 1 && capacity <= QCU_MAX_RHS, QCU_ERR_INVALID_ARGUMENT, "slot capacity must be in 1..256");
   QCU_REQUIRE(q.solver == 0 || q.solver == 1, QCU_ERR_INVALID_ARGUMENT, "unknown solver");
   QCU_REQUIRE(prec_valid(q.inner_prec), QCU_ERR_INVALID_ARGUMENT, "bad inner precision");
-  QCU_REQUIRE(!(s.has_clover() && prec_site_major(q.inner_prec)), QCU_ERR_UNSUPPORTED,
+  QCU_REQUIRE(!(q.clover && prec_site_major(q.inner_prec)), QCU_ERR_UNSUPPORTED,
               "clover: site-major BF16 fields are not supported");
   QCU_REQUIRE(!prec_site_major(q.inner_prec) || capacity % 4 == 0, QCU_ERR_UNSUPPORTED,
               "site-major BF16 inner fields take the tensor-core dslash: the RHS count must be a multiple of 4");
@@ -266,6 +266,12 @@ SlotEngine::SlotEngine(Session& s, int capacity, const SolveRequest& q, const st
     wop_ = s.alloc_field(t + "wop", op_, n_);
   }
   tmpop_ = s.alloc_field(t + "tmpop", op_, n_);
+  // BF16 operator fields are internal: they take the site-major layout where
+  // the tensor-core dslash on it is measured faster (same bytes either way)
+  if (op_ == PREC_BF16 && !q.clover && s.prefer_site_major(pop_, qop_)) {
+    op_ = PREC_BF16S;
+    for (FieldView* f : {&pop_, &qop_, &wop_, &tmpop_}) f->prec = PREC_BF16S;
+  }
   cl_ = q.clover;
   QCU_REQUIRE(!cl_ || s.has_clover(), QCU_ERR_NO_OPERATOR, "clover solve requested but no clover field loaded");
   if (cl_) {
