@@ -123,6 +123,14 @@ void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int n
   encode(m, ptr, dims, strides, box);
 }
 
+void tma_encode_gauge_rows(CUtensorMap* m, const void* ptr, int ebytes, int vh, int nn, int hx) {
+  const cuuint64_t blk = (cuuint64_t)vh * nn * ebytes;  // one (mu, parity) block, bytes
+  const cuuint64_t dims[3] = {blk / 4, 1, 8};
+  const cuuint64_t strides[2] = {blk, blk};
+  const cuuint32_t box[3] = {(cuuint32_t)(hx * nn * ebytes / 4), 1, 1};
+  encode(m, ptr, dims, strides, box);
+}
+
 bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major) {
   // byte strides of colour, spin and site
   const cuuint64_t cs = site_major ? (cuuint64_t)nrhs * 4 : (cuuint64_t)vh * nrhs * 4;

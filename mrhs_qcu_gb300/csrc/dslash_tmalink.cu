@@ -15,8 +15,10 @@ bool tmalink_runs(const DslashArgs& A, int R, int ebytes, int nn) {
   // one CTA per row; the instances cap registers at 128, so at most 512 threads per CTA
   const int64_t threads = (int64_t)hx * (A.nrhs / R);
   if (threads < 1 || threads > 512) return false;
-  // TMA: box inner extent a multiple of 16 bytes and at most 256 elements, 16-byte aligned rows and strides
-  if ((hx * ebytes) % 16 || hx * ebytes / 4 > 256 || nn > 256) return false;
+  // TMA: box inner extent a multiple of 16 bytes and at most 256 4-byte elements, 16-byte aligned
+  // rows and strides (full links: inner extent hx complexes; two-row links: 6 hx, contiguous)
+  const int inner = (nn == 6 ? 6 : 1) * hx * ebytes;
+  if (inner % 16 || inner / 4 > 256 || nn > 256) return false;
   const void* g = (nn == 6) ? A.gauge12 : A.gauge;
   if (!g || (uintptr_t)g % 16 || ((int64_t)A.geo.vh * ebytes) % 16) return false;
   if (tmalink_smem_bytes(nn, hx, ebytes) > 200 * 1024) return false;

@@ -205,6 +205,7 @@ __global__ void compress_gauge_kernel(const double2* __restrict__ src, void* dst
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
     const int64_t blk = i / (6 * vh), rem = i - blk * 6 * vh;  // rem = comp * vh + site, comp < 6
+    const int64_t comp = rem / vh, site = rem - comp * vh;
     const double2 v = src[blk * 9 * vh + rem];
     E e;
     if constexpr (P == PREC_DOUBLE) {
@@ -214,7 +215,7 @@ __global__ void compress_gauge_kernel(const double2* __restrict__ src, void* dst
     } else {
       e = S::from_c(make_float2((float)v.x, (float)v.y));
     }
-    static_cast<E*>(dst)[i] = e;
+    static_cast<E*>(dst)[blk * 6 * vh + site * 6 + comp] = e;  // [8][Vh][6]: one link's six contiguous
   }
 }
 

@@ -118,14 +118,16 @@ def _pin(R, minb, pk, rc, lt, block=64):
 
 @pytest.mark.parametrize("prec,rc,L,nrhs", [
     (1, 1, (4, 4, 4, 8), 12), (1, 0, (4, 4, 4, 8), 2), (1, 1, (12, 4, 6, 4), 12), (1, 1, (16, 6, 4, 10), 64),
-    (1, 0, (8, 8, 8, 16), 24), (1, 1, (8, 8, 8, 16), 4), (4, 1, (8, 8, 8, 16), 12), (4, 1, (16, 6, 4, 10), 64)])
+    (1, 0, (8, 8, 8, 16), 24), (1, 1, (8, 8, 8, 16), 4), (4, 1, (8, 8, 8, 16), 12), (4, 1, (16, 6, 4, 10), 64),
+    (1, 1, (6, 4, 4, 4), 12), (4, 1, (4, 4, 4, 8), 4)])
 def test_link_staged_kernel(cuda, qcu_lib, prec, rc, L, nrhs):
     """The register kernel with its links staged by TMA into shared memory
     (one CTA per x-row, eight boxes on eight mbarriers): against the oracle on
-    both parities, dagger flags and antiperiodic t, for rows of 2..8 sites,
-    1..32 RHS groups, full and two-row links, FP32 and BF16 storage; launched
-    (not a fallback) and bit-identical to the register kernel of the same R
-    and link form."""
+    both parities, dagger flags and antiperiodic t, for rows of 2..8 sites
+    (3 with two-row FP32 links, whose contiguous row is 144 bytes), 1..32 RHS
+    groups, full and two-row links, FP32 and BF16 storage; launched (not a
+    fallback) and bit-identical to the register kernel of the same R and
+    link form."""
     Q = qcu_lib
     g = S.random_gauge(L, 3, seed=600 + nrhs)
     psi = S.random_fermions(L, 3, nrhs, seed=601 + nrhs)
@@ -145,16 +147,18 @@ def test_link_staged_kernel(cuda, qcu_lib, prec, rc, L, nrhs):
         os.environ.pop("QCU_DSLASH_CONFIG", None)
 
 
-@pytest.mark.parametrize("L,prec", [((6, 4, 4, 4), 1), ((4, 4, 4, 8), 4), ((12, 4, 6, 4), 4)])
-def test_link_staged_kernel_falls_back(cuda, qcu_lib, L, prec):
-    """A row whose links are not a multiple of 16 bytes (X/2 = 3 sites in
-    FP32, 2 or 6 sites in BF16) cannot be a TMA box: the pinned link-staged
-    shape runs the register kernel, with the oracle's result."""
+@pytest.mark.parametrize("L,prec,rc", [((6, 4, 4, 4), 1, 0), ((6, 4, 4, 4), 4, 1), ((10, 4, 2, 4), 4, 1)])
+def test_link_staged_kernel_falls_back(cuda, qcu_lib, L, prec, rc):
+    """A row whose links are not a whole number of 16-byte units cannot be a
+    TMA box: full FP32 links of X/2 = 3 sites (24 bytes per component row),
+    two-row BF16 links of 3 or 5 sites (72 or 120 contiguous bytes).  The
+    pinned link-staged shape runs the register kernel, with the oracle's
+    result."""
     Q = qcu_lib
     g = S.random_gauge(L, 3, seed=610)
     psi = S.random_fermions(L, 3, 4, seed=611)
-    minb = [s[1] for s in Q.dslash_kernels(prec, 3) if s[0] == 2 and s[2] == 1 and s[4] == 1 and s[5] == 1][0]
-    os.environ["QCU_DSLASH_CONFIG"] = _pin(2, minb, 1, 1, 1)
+    minb = [s[1] for s in Q.dslash_kernels(prec, 3) if s[0] == 2 and s[2] == 1 and s[4] == rc and s[5] == 1][0]
+    os.environ["QCU_DSLASH_CONFIG"] = _pin(2, minb, 1, rc, 1)
     try:
         got = abi_dslash(cuda, Q, psi, g, L, 1, 0, prec, antiperiodic_t=True)
         assert Q.last_dslash_shape()[5] == 0
