@@ -306,7 +306,7 @@ def run_gpu(args):
     peak, peak_kind = measured_peaks()
     bpu = bytes_per_site_rhs(prec, n, nrhs)
     achieved = bpu * units / (ms_local * 1e-3) / 1e9
-    tcs_rings = {4: (4, 3), 5: (6, 3), 6: (3, 2)}  # (TMA stages, B buffers) of variants 4-6
+    tcs_rings = {4: (4, 3), 5: (6, 3), 6: (3, 2), 7: (8, 3), 8: (6, 4)}  # (TMA stages, B buffers) of variants 4-8
     kernel = (("wilson_tcs_kernel<N=%d,stages=%d,bbufs=%d> (tcgen05, %s)"
                % ((n,) + tcs_rings[-stages] + ("site-major" if prec == 5 else "component-major",)))
               if stages <= -4 else

@@ -241,14 +241,16 @@ int qcuMeasureFmaRate(int precision, double *tflops);
  * a tensor-core (tcgen05) kernel, BF16 only: -1 projected half-spinor
  * operands with direct loads, -2 / -3 the same with a TMA ring of that depth,
  * -4 / -5 / -6 the neighbour spinor block as the MMA operand (warp-specialised,
- * TMA and B rings of different depths; nrhs a multiple of 4); recon = 1 reads
+ * TMA and B rings of different depths; nrhs a multiple of 4), -7 / -8 the
+ * same with deeper rings of half-size stages (tiles of at most 32 RHS);
+ * recon = 1 reads
  * SU(3) links as two rows and reconstructs the third (used only when the
  * loaded gauge is SU(3) to the precision's rounding); linktma = 1 is the
  * register kernel with one CTA per x-row whose links are staged by TMA into
  * shared memory (used when X/2 x the complex size is a multiple of 16 bytes
  * and X/2 x nrhs / R <= 512).  Any shape can be pinned with
  * QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon,linktma"
- * (tensor = 1..6 for the tensor-core variants). */
+ * (tensor = 1..8 for the tensor-core variants). */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 
 typedef struct QcuSolverParam_s {

@@ -103,7 +103,7 @@ bool tc_runs(const DslashArgs& A_in, int prec, int N, int variant) {
   if (variant >= 4) {
     TcsDslashArgs T4;
     CUtensorMap m;
-    return tcs_plan(A, N, &T4, &m);
+    return tcs_plan(A, N, &T4, &m) && T4.halves <= tcs_halves(variant);
   }
   return (variant < 2 || (uintptr_t)A.in % 16 == 0) &&
          tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);
@@ -127,7 +127,7 @@ void launch_dslash(const DslashArgs& A_in, int prec, int N, const DslashConfig& 
   if (A.site_major && !(cfg.tc >= 4 && tc_runs(A, prec, N, cfg.tc))) {
     // site-major fields have only the spinor-operand tensor-core kernels: the first that runs
     cfg = DslashConfig{};
-    for (int v = 4; v <= 6 && !cfg.tc; v++)
+    for (int v = 4; v <= kTcVariants && !cfg.tc; v++)
       if (tc_runs(A, prec, N, v)) cfg.tc = v;
     QCU_REQUIRE(cfg.tc, QCU_ERR_UNSUPPORTED,
                 "site-major BF16 fields need the tensor-core dslash: nrhs a multiple of 4, N = 2..8, 16-byte "

@@ -26,28 +26,32 @@ int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols = 32, int
 // offsets, and a field map the driver accepts).
 bool tcs_plan(const DslashArgs& A, int N, TcsDslashArgs* T, CUtensorMap* map_in);
 
-// ring depths of the spinor-operand variants 4, 5, 6: (TMA stages, B buffers)
-constexpr int tcs_stages(int variant) { return variant == 5 ? 6 : variant == 6 ? 3 : 4; }
-constexpr int tcs_bbufs(int variant) { return variant == 6 ? 2 : 3; }
+// ring depths of the spinor-operand variants 4-8: (TMA stages, B buffers, A
+// halves of 32 RHS per stage).  Variants 7 and 8 hold one half per stage, so
+// their deeper rings fit the same shared memory; they take tiles of at most
+// 32 RHS (nrhs <= 32, or RHS counts that split into such tiles).
+constexpr int tcs_stages(int variant) { return variant == 5 ? 6 : variant == 6 ? 3 : variant == 7 ? 8 : variant == 8 ? 6 : 4; }
+constexpr int tcs_bbufs(int variant) { return variant == 6 ? 2 : variant == 8 ? 4 : 3; }
+constexpr int tcs_halves(int variant) { return variant >= 7 ? 1 : 2; }
 
 template <int N, int V>
 void launch_wilson_tcs(const DslashArgs& A, cudaStream_t st) {
-  constexpr int NST = tcs_stages(V), NB = tcs_bbufs(V);
+  constexpr int NST = tcs_stages(V), NB = tcs_bbufs(V), HV = tcs_halves(V);
   TcsDslashArgs T;
   CUtensorMap mi;
-  QCU_REQUIRE(tcs_plan(A, N, &T, &mi), QCU_ERR_UNSUPPORTED,
+  QCU_REQUIRE(tcs_plan(A, N, &T, &mi) && T.halves <= HV, QCU_ERR_UNSUPPORTED,
               "tensor-core dslash: arguments outside the kernel's limits");
   T.A = A;
   T.err = tma_error_flag();
-  const size_t smem = tcs::smem_bytes(NST, NB);
-  const void* k = reinterpret_cast<const void*>(&wilson_tcs_kernel<N, NST, NB>);
+  const size_t smem = tcs::smem_bytes(NST, NB, HV);
+  const void* k = reinterpret_cast<const void*>(&wilson_tcs_kernel<N, NST, NB, HV>);
   static size_t smem_set = 0;
   if (smem > 48 * 1024 && smem > smem_set) {
     QCU_CHECK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     smem_set = smem;
   }
   const int grid = tc_grid(k, T.ntiles, smem, (int)tcs::kTmemCols, tcs::kThreads);
-  wilson_tcs_kernel<N, NST, NB><<<grid, tcs::kThreads, smem, st>>>(T, mi);
+  wilson_tcs_kernel<N, NST, NB, HV><<<grid, tcs::kThreads, smem, st>>>(T, mi);
   tma_note_launch();
 }
 
@@ -77,7 +81,9 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
 
 // variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages (projected
 // half-spinor operands, dslash_tc.cuh); 4 / 5 / 6 = the spinor-operand kernel
-// (dslash_tcs.cuh) with (TMA stages, B buffers) = (4, 3) / (6, 3) / (3, 2)
+// (dslash_tcs.cuh) with (TMA stages, B buffers) = (4, 3) / (6, 3) / (3, 2);
+// 7 / 8 = the same with one 32-RHS half per stage, (8, 3) / (6, 4)
+constexpr int kTcVariants = 8;
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
 void register_tc(int prec, int N, int variant, TcLauncher fn);
 TcLauncher find_tc(int prec, int N, int variant = 1);

@@ -1,5 +1,5 @@
 // Instances of the spinor-operand tensor-core dslash (dslash_tcs.cuh):
-// tensor-core variants 4 / 5 / 6 (ring depths in dslash_tc.h), BF16 in either
+// tensor-core variants 4-8 (ring depths in dslash_tc.h), BF16 in either
 // layout, N = 3..8.
 #include "dslash_tc.h"
 
@@ -13,6 +13,8 @@ void register_n() {
     register_tc(prec, N, 4, &launch_wilson_tcs<N, 4>);
     register_tc(prec, N, 5, &launch_wilson_tcs<N, 5>);
     register_tc(prec, N, 6, &launch_wilson_tcs<N, 6>);
+    register_tc(prec, N, 7, &launch_wilson_tcs<N, 7>);
+    register_tc(prec, N, 8, &launch_wilson_tcs<N, 8>);
   }
 }
 

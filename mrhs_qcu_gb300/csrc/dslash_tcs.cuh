@@ -66,22 +66,28 @@ struct TcsDslashArgs {
 
 namespace tcs {
 
-constexpr uint32_t kHalfBytes = 4096;               // 4 spins x 8 colours x 128 B
-constexpr uint32_t kABytes = 2 * kHalfBytes;        // M = 128 rows
+constexpr uint32_t kHalfBytes = 4096;               // 4 spins x 8 colours x 128 B (32 RHS)
 constexpr uint32_t kLinkBytes = 1024;               // one link in row form (256 B), 1 KB keeps stages aligned
-constexpr uint32_t kStageBytes = kABytes + kLinkBytes;
 constexpr uint32_t kBBytes = 4096;                  // 64 (n) x 32 (k) BF16, K-major
 constexpr uint32_t kTmemCols = 128;  // two accumulators of 64 columns
+// A stage holds HV A halves of 32 RHS (M rows 64 h .. 64 h + 63) and the
+// link.  With HV = 1 (tiles of at most 32 RHS) the MMA's rows 64-127 read
+// the 4 KB after the half, whatever lies there: their accumulator lanes are
+// never stored, and the read stays inside the CTA's shared memory (the B
+// buffers follow the last stage).
+__host__ __device__ constexpr uint32_t stage_bytes(int hv) { return (uint32_t)hv * kHalfBytes + kLinkBytes; }
 
 // offsets from the 1024-byte aligned base of dynamic shared memory: TMA
 // stages, B buffers, barriers
-__host__ __device__ constexpr uint32_t b_off(int nst) { return (uint32_t)nst * kStageBytes; }
-__host__ __device__ constexpr uint32_t bar_off(int nst, int nb) { return b_off(nst) + (uint32_t)nb * kBBytes; }
+__host__ __device__ constexpr uint32_t b_off(int nst, int hv) { return (uint32_t)nst * stage_bytes(hv); }
+__host__ __device__ constexpr uint32_t bar_off(int nst, int nb, int hv) { return b_off(nst, hv) + (uint32_t)nb * kBBytes; }
 // barriers: ring_full[nst], ring_empty[nst], b_full[nb], b_empty[nb],
 // tmem_full[2], tmem_empty[2], drain; then the tensor-memory slot and the abort flag
-__host__ __device__ constexpr uint32_t slot_off(int nst, int nb) { return bar_off(nst, nb) + 8u * (2 * nst + 2 * nb + 5); }
+__host__ __device__ constexpr uint32_t slot_off(int nst, int nb, int hv) {
+  return bar_off(nst, nb, hv) + 8u * (2 * nst + 2 * nb + 5);
+}
 // + 1024 bytes to align the base
-__host__ __device__ constexpr uint32_t smem_bytes(int nst, int nb) { return slot_off(nst, nb) + 16 + 1024; }
+__host__ __device__ constexpr uint32_t smem_bytes(int nst, int nb, int hv) { return slot_off(nst, nb, hv) + 16 + 1024; }
 constexpr int kThreads = 320;
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, A MN-major (bit
@@ -193,11 +199,13 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, vo
 // bytes from arrays Vh x nrhs x 4 bytes apart, which the copy engine serves
 // at about half the rate when a hop's block is 8 KB.  The
 // links come from A.gauge_tc (BF16 row form, one 256-byte bulk copy per hop).
-template <int N, int NST, int NB>
+template <int N, int NST, int NB, int HV>
 __global__ void __launch_bounds__(tcs::kThreads, 4)
     wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
   static_assert(N >= 2 && N <= 8, "colours are padded to 8");
   static_assert(NST >= 2 && NST <= 8 && NB >= 2 && NB <= 4, "ring depths");
+  static_assert(HV == 1 || HV == 2, "A halves per stage");
+  constexpr uint32_t kStage = tcs::stage_bytes(HV), kA = (uint32_t)HV * tcs::kHalfBytes;
   using namespace detail;
   const DslashArgs& A = T.A;
   extern __shared__ unsigned char smem_raw[];
@@ -205,15 +213,15 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
   const uint32_t raw0 = tma::smem_u32(smem_raw);
   const uint32_t smem0 = (raw0 + 1023u) & ~1023u;
   unsigned char* smem = smem_raw + (smem0 - raw0);
-  const uint32_t ring_full = smem0 + tcs::bar_off(NST, NB);
+  const uint32_t ring_full = smem0 + tcs::bar_off(NST, NB, HV);
   const uint32_t ring_empty = ring_full + 8 * NST;
   const uint32_t b_full = ring_empty + 8 * NST;
   const uint32_t b_empty = b_full + 8 * NB;
   const uint32_t tmem_full = b_empty + 8 * NB;
   const uint32_t tmem_empty = tmem_full + 16;
   const uint32_t drain = tmem_empty + 16;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + tcs::slot_off(NST, NB));
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + tcs::slot_off(NST, NB) + 8);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + tcs::slot_off(NST, NB, HV));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + tcs::slot_off(NST, NB, HV) + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   if (tid == 0) {
@@ -289,8 +297,8 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
         const bool zim = off && imag;
         // link rows in the stage: row (part, a) of W = U (forward) or of U^T
         // (backward, whose conjugation flips the sign of the Im part)
-        const unsigned char* wr = smem + st * tcs::kStageBytes + tcs::kABytes;
-        unsigned char* bbuf = smem + tcs::b_off(NST) + b * tcs::kBBytes;
+        const unsigned char* wr = smem + st * kStage + kA;
+        unsigned char* bbuf = smem + tcs::b_off(NST, HV) + b * tcs::kBBytes;
 #pragma unroll
         for (int part = 0; part < 2; part++) {
           uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -336,8 +344,8 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
                tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
           if (!ok) break;
           tc::fence_after();
-          const uint32_t sa = smem0 + st * tcs::kStageBytes;
-          const uint32_t sb = smem0 + tcs::b_off(NST) + b * tcs::kBBytes;
+          const uint32_t sa = smem0 + st * kStage;
+          const uint32_t sb = smem0 + tcs::b_off(NST, HV) + b * tcs::kBBytes;
           const uint32_t d = tmem + acc * 64u;
           // K step j: input spins 2j, 2j + 1 (two 1 KB swizzle atoms of A, two 128 B core-matrix columns of B)
           tc::mma_bf16(d, tcs::a_desc(sa), tcs::b_desc(sb), tcs::kIdesc, h > 0);
@@ -375,13 +383,13 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           }
           const uint32_t nbq = sc.nb(A, d);
           const uint32_t lsite = (d & 1) ? nbq : st_site, lpar = (d & 1) ? 1u - p : p;
-          const uint32_t bar = ring_full + 8 * st, dst = smem0 + st * tcs::kStageBytes;
+          const uint32_t bar = ring_full + 8 * st, dst = smem0 + st * kStage;
           tma::mbar_expect_tx(bar, tx);
           for (int h = 0; h < T.halves; h++)
             tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0,
                          (int)nbq, bar, keep);
           // form 0 (rows of U) for forward hops, form 1 (rows of U^T) for backward ones
-          tcs::bulk_load(dst + tcs::kABytes,
+          tcs::bulk_load(dst + kA,
                          gtc + ((uint64_t)((d & 1) * 8 + 2 * (d >> 1) + lpar) * vh + lsite) * kLink, kLink, bar);
         }
       }

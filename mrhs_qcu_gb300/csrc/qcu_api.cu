@@ -647,7 +647,7 @@ int qcuDslashKernels(int precision, int nColors, int* shapes, int max_shapes, in
     int tr[32], ts[32];
     const int nt = qcu::tma_options(precision, nColors, tr, ts, 32);
     for (int i = 0; i < nt; i++) put(tr[i], 0, 0, ts[i], 0, 0);
-    for (int v = 1; v <= 6; v++)
+    for (int v = 1; v <= qcu::kTcVariants; v++)
       if (qcu::find_tc(precision, nColors, v)) put(1, 0, 0, -v, 0, 0);
     *count = n;
   });

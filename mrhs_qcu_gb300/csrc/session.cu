@@ -236,7 +236,7 @@ DslashConfig Autotuner::tune(const DslashArgs& A, int prec, int N, cudaStream_t 
   // the tensor-core kernel, where these arguments fit it; at N <= 4 the
   // CUDA-core kernels were faster at every RHS count measured (16^3x32, nrhs
   // 16-64), so component-major fields do not time them there
-  for (int variant = 1; variant <= 6; variant++) {
+  for (int variant = 1; variant <= kTcVariants; variant++) {
     if (!tc_runs(A, prec, N, variant)) continue;
     if (N <= 4 && !prec_site_major(prec)) continue;
     DslashConfig c;

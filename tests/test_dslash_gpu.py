@@ -199,7 +199,7 @@ def test_link_staged_kernel_in_masked_solve(cuda, qcu_lib):
             assert res < 2 * tol, (r, res)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6, 7, 8])
 @pytest.mark.parametrize("n,nrhs", [(4, 16), (8, 16), (6, 24), (8, 64), (5, 128), (3, 32), (7, 36), (8, 8)])
 def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
     """The tcgen05 kernels (BF16 storage and operands, FP32 accumulation in
@@ -207,7 +207,9 @@ def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
     antiperiodic t, RHS counts that fill the 128 MMA rows, leave them partly
     empty, take two tiles, or end inside the second 32-RHS box.  Variants 1-3
     are the projected half-spinor kernel (N >= 4; the TMA ring for N = 4, 6,
-    8), 4-6 the spinor-operand kernel with 2-4 ring stages."""
+    8), 4-6 the spinor-operand kernel with 2-4 ring stages, 7-8 the same with
+    deeper rings of one 32-RHS half per stage (launched for tiles of at most
+    32 RHS; larger tiles run another kernel)."""
     L = (4, 4, 4, 8)
     g = S.random_gauge(L, n, seed=90 + n)
     psi = S.random_fermions(L, n, nrhs, seed=91)
@@ -217,9 +219,12 @@ def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
         pytest.skip("the projected kernel's TMA ring is compiled for N = 4, 6, 8")
     os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
     try:
+        tile = max(t for t in range(4, 65, 4) if nrhs % t == 0)  # RHS per tile of the spinor-operand kernel
         for parity, dag in ((0, 0), (1, 1), (1, 0)):
             got = abi_dslash(cuda, qcu_lib, psi, g, L, parity, dag, 4, antiperiodic_t=True)
             assert rel(got, O.dslash(psi, g, L, parity, dag, True)) < TOL[4], (parity, dag)
+            if variant >= 4 and (variant <= 6 or tile <= 32):
+                assert qcu_lib.last_dslash_shape()[3] == -variant
         assert qcu_lib.tune_dslash(nrhs, 4)[4] == -variant  # the pinned shape is this tensor-core variant
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]

@@ -66,7 +66,7 @@ def test_pack_is_the_transposed_component_major_field(cuda, qcu_lib, n, nrhs):
     del dg
 
 
-@pytest.mark.parametrize("variant", [4, 5, 6])
+@pytest.mark.parametrize("variant", [4, 5, 6, 7, 8])
 @pytest.mark.parametrize("n,nrhs", [(3, 4), (4, 16), (6, 32), (8, 64), (5, 36), (8, 8), (7, 12)])
 def test_dslash_site_major_bitwise_and_oracle(cuda, qcu_lib, n, nrhs, variant):
     """Both parities and dagger flags, antiperiodic t; RHS counts that fill
@@ -76,13 +76,17 @@ def test_dslash_site_major_bitwise_and_oracle(cuda, qcu_lib, n, nrhs, variant):
     L = (4, 4, 4, 8)
     g = S.random_gauge(L, n, seed=510 + n)
     psi = S.random_fermions(L, n, nrhs, seed=511)
-    os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
+    # variants 7-8 take tiles of at most 32 RHS; larger tiles run the first variant that fits (4)
+    ran = variant if variant <= 6 or nrhs <= 32 else 4
     try:
         for parity, dag in ((0, 0), (1, 1), (1, 0)):
+            os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % variant
             got = abi_dslash(torch, Q, psi, g, L, parity, dag, SITE, antiperiodic_t=True)
-            assert Q.last_dslash_shape()[3] == -variant
+            assert Q.last_dslash_shape()[3] == -ran
             assert rel(got, O.dslash(psi, g, L, parity, dag, True)) < TOL[BF16], (parity, dag)
+            os.environ["QCU_DSLASH_CONFIG"] = "1,0,0,0,0,0,%d" % ran
             other = abi_dslash(torch, Q, psi, g, L, parity, dag, BF16, antiperiodic_t=True)
+            assert Q.last_dslash_shape()[3] == -ran
             assert np.array_equal(got, other), (parity, dag)
     finally:
         del os.environ["QCU_DSLASH_CONFIG"]
@@ -94,8 +98,8 @@ def test_tuned_site_major_is_a_tensor_core_shape(cuda, qcu_lib):
     torch, Q = cuda, qcu_lib
     L, n, nrhs = (4, 4, 4, 8), 4, 16
     dg = _setup(torch, Q, L, n, S.random_gauge(L, n, seed=520))
-    assert Q.tune_dslash(nrhs, SITE)[4] in (-4, -5, -6)
-    assert sorted(k[3] for k in Q.dslash_kernels(SITE, n)) == [-6, -5, -4]
+    assert Q.tune_dslash(nrhs, SITE)[4] in (-4, -5, -6, -7, -8)
+    assert sorted(k[3] for k in Q.dslash_kernels(SITE, n)) == [-8, -7, -6, -5, -4]
     del dg
 
 
