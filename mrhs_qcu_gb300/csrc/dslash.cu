@@ -109,6 +109,30 @@ bool tc_runs(const DslashArgs& A_in, int prec, int N, int variant) {
          tc_plan(prec, N, A.geo, A.nrhs, tc_ring_stages(variant), &T, &smem);
 }
 
+void plan_site_order(DslashArgs& B, int prec, int N) {
+  // Measured at 32^3x64 FP32 SU(3) (register kernel, G site*RHS/s): nrhs 12
+  // field order 17.8, slabs of 16 / 8 / 4 planes 19.0 / 19.0 / 18.5; nrhs 24
+  // 15.9, 17.8 / 19.1 / 18.8.  The best slab keeps three slab-slices of input
+  // and output within 28-57 MB; thinner slabs re-read more of their z faces.
+  const Geometry& g = B.geo;
+  const int64_t site_bytes = (int64_t)2 * 4 * N * B.nrhs * prec_complex_bytes(prec);  // in + out
+  const int64_t field_bytes = site_bytes * g.vh;
+  B.zb = 0;
+  B.stream_out = field_bytes > ((int64_t)96 << 20) ? 1 : 0;  // larger than L2: the output is not re-read from it
+  if (field_bytes <= ((int64_t)96 << 20)) return;
+  int zb = g.L[2];
+  while (zb > 1 && (int64_t)3 * g.plane * zb * site_bytes > ((int64_t)64 << 20)) {
+    int d = zb - 1;
+    while (d > 1 && g.L[2] % d) d--;  // the next smaller divisor of Lz
+    zb = d;
+  }
+  if (zb >= g.L[2]) return;  // whole t-slices already fit
+  B.zb = (uint32_t)zb;
+  B.div_plane = FastDiv((uint32_t)g.plane);
+  B.div_zb = FastDiv((uint32_t)zb);
+  B.div_lt = FastDiv((uint32_t)g.L[3]);
+}
+
 namespace {
 DslashConfig no_launch() {
   DslashConfig c;
@@ -204,6 +228,7 @@ void launch_dslash(const DslashArgs& A_in, int prec, int N, const DslashConfig& 
   B.div_groups = FastDiv((uint32_t)(A.nrhs / cfg.R));
   B.af = (float)A.a;
   B.bf = (float)A.b;
+  if (!cfg.lt) plan_site_order(B, prec, N);  // the link-staged kernel walks x-rows in its own order
   fn(B, cfg.block, st);
   QCU_CHECK_CUDA(cudaGetLastError());
   cfg.tma = cfg.rcta = cfg.tc = 0;
@@ -250,6 +275,7 @@ int launch_dslash_segments(const std::vector<DslashArgs>& all, int prec, int N, 
       B.div_groups = FastDiv((uint32_t)(B.nrhs / cfg.R));
       B.af = (float)B.a;
       B.bf = (float)B.b;
+      plan_site_order(B, prec, N);
       S.A[i] = B;
       blocks += ((int64_t)B.geo.vh * (B.nrhs / cfg.R) + cfg.block - 1) / cfg.block;
     }

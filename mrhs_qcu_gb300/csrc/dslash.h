@@ -46,6 +46,10 @@ struct DslashConfig {
   int lt = 0;    // 1: the register kernel with its links staged by TMA (one CTA per x-row)
 };
 
+// The register kernel's site order and output store policy for B (prec, N):
+// slabs of z-planes where whole t-slices of the field overflow L2, evict-first
+// output stores where the field is larger than L2.
+void plan_site_order(DslashArgs& B, int prec, int N);
 // The shape launch_dslash last launched on the calling thread (after its
 // fallbacks: a pinned shape the arguments rule out runs another kernel).
 DslashConfig last_launched_dslash();

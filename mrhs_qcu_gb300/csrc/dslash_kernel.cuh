@@ -48,6 +48,14 @@ struct DslashArgs {
   int antiperiodic_t;
   FastDiv div_groups;    // G = nrhs / R
   int site_major = 0;    // spinor fields in the site-major layout (PREC_BF16S; set by launch_dslash)
+  // Site order of the register kernel (set by launch_dslash): slabs of zb
+  // z-planes, t slowest within a slab, so that the reads of an input site
+  // (as the x, y, z neighbour of its own slice and the t neighbour of the
+  // slices on either side) fall within about three slab-slices instead of
+  // three whole t-slices, and stay in L2.  zb = 0: the field's own order.
+  uint32_t zb = 0;
+  FastDiv div_plane, div_zb, div_lt;
+  int stream_out = 0;  // output stores marked evict-first (the output is not re-read by the launch)
 };
 
 namespace detail {
@@ -112,12 +120,17 @@ struct Vec {
       for (int i = 0; i < nv; i++) d[i] = q[i];
     }
   }
-  __device__ __forceinline__ static void store(E* p, const E (&v)[R]) {
+  __device__ __forceinline__ static void store(E* p, const E (&v)[R], bool cs = false) {
     if constexpr (vbytes == 16) {
       uint4* q = reinterpret_cast<uint4*>(p);
       const uint4* s = reinterpret_cast<const uint4*>(v);
 #pragma unroll
-      for (int i = 0; i < nv; i++) q[i] = s[i];
+      for (int i = 0; i < nv; i++) {
+        if (cs)
+          __stcs(q + i, s[i]);
+        else
+          q[i] = s[i];
+      }
     } else if constexpr (vbytes == 8) {
       uint2* q = reinterpret_cast<uint2*>(p);
       const uint2* s = reinterpret_cast<const uint2*>(v);
@@ -653,7 +666,7 @@ __device__ __forceinline__ void store_out(C2<typename Store<P>::real> (&acc)[4][
           float2 v = make_float2(acc[sp][a][r].x * inv[r], acc[sp][a][r].y * inv[r]);
           ov.v[r] = S::from_c(v);
         }
-        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v);
+        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v, A.stream_out != 0);
       }
   } else {
 #pragma unroll
@@ -668,7 +681,7 @@ __device__ __forceinline__ void store_out(C2<typename Store<P>::real> (&acc)[4][
           e.y = acc[sp][a][r].y;
           ov.v[r] = e;
         }
-        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v);
+        Vec<E, R>::store(out + (o + (uint32_t)(sp * N + a) * cs), ov.v, A.stream_out != 0);
       }
   }
 }
@@ -703,6 +716,7 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
   uint32_t site, grp;
   A.div_groups.divmod(gid, site, grp);
   if (site >= (uint32_t)A.geo.vh) return;
+  uint32_t rest, xh, y, z, t;
   const uint32_t rhs0 = grp * R;
   if (A.mask) {
     bool any = false;
@@ -711,11 +725,20 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
     if (!any) return;
   }
 
-  uint32_t rest, xh, y, z, t;
-  A.geo.div_hx.divmod(site, rest, xh);
-  uint32_t rest2;
-  A.geo.div_y.divmod(rest, rest2, y);
-  A.geo.div_z.divmod(rest2, t, z);
+  if (A.zb) {  // s-th site of the slab order
+    uint32_t q, r, q2, zz, slab;
+    A.div_plane.divmod(site, q, r);
+    A.div_zb.divmod(q, q2, zz);
+    A.div_lt.divmod(q2, slab, t);
+    z = slab * A.zb + zz;
+    A.geo.div_hx.divmod(r, y, xh);
+    site = (t * (uint32_t)A.geo.L[2] + z) * (uint32_t)A.geo.plane + r;
+  } else {
+    uint32_t rest, rest2;
+    A.geo.div_hx.divmod(site, rest, xh);
+    A.geo.div_y.divmod(rest, rest2, y);
+    A.geo.div_z.divmod(rest2, t, z);
+  }
   const uint32_t hx = A.geo.hx, Ly = A.geo.L[1], Lz = A.geo.L[2], Lt = A.geo.L[3];
   const uint32_t p = A.parity;
   const uint32_t eo = (y + z + t) & 1u;
