@@ -250,7 +250,10 @@ int qcuMeasureFmaRate(int precision, double *tflops);
  * shared memory (used when X/2 x the complex size is a multiple of 16 bytes
  * and X/2 x nrhs / R <= 512).  Any shape can be pinned with
  * QCU_DSLASH_CONFIG="R,block,reg_cap,packed,stages,rcta,tensor,recon,linktma"
- * (tensor = 1..8 for the tensor-core variants). */
+ * (tensor = 1..8 for the tensor-core variants).  Where whole t-slices of the
+ * fields overflow L2, the register kernels walk the lattice in slabs of
+ * z-planes (t slowest within a slab); QCU_DSLASH_ZSLAB=<planes> overrides the
+ * slab height (0: the field's own order). */
 int qcuDslashKernels(int precision, int nColors, int *shapes, int max_shapes, int *count);
 
 typedef struct QcuSolverParam_s {

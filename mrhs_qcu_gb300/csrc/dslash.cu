@@ -1,5 +1,6 @@
 // Dslash registry and launch (see dslash.h).
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 
@@ -125,6 +126,11 @@ void plan_site_order(DslashArgs& B, int prec, int N) {
     int d = zb - 1;
     while (d > 1 && g.L[2] % d) d--;  // the next smaller divisor of Lz
     zb = d;
+  }
+  // QCU_DSLASH_ZSLAB=<planes> overrides the choice (0: the field's order)
+  if (const char* e = getenv("QCU_DSLASH_ZSLAB")) {
+    const int v = atoi(e);
+    zb = (v > 0 && g.L[2] % v == 0) ? v : g.L[2];
   }
   if (zb >= g.L[2]) return;  // whole t-slices already fit
   B.zb = (uint32_t)zb;
