@@ -8,6 +8,8 @@
   nrhs = 12, kappa = 0.12, point sources, tolerance 1e-10), FP32 and FP16
   inner, each RHS checked by the oracle's FP64 true residual of the full
   Wilson system.
+* 16x16x12x32 SU(3), nrhs 128 (fields larger than L2): the register
+  kernel's slab site order, bit-identical across slab heights.
 * 16^3 x 32 SU(N), N = 4, 6, 8, nrhs 16 / 32 / 64: the CUDA-core kernels
   (FP32, BF16) and the tensor-core kernels (BF16, component- and site-major
   fields), and a masked BiCGStab to 1e-8 (one source 1e-4 smaller, one
@@ -163,3 +165,57 @@ def test_sun_bicgstab_masks(cuda, qcu_lib, n, inner):
             continue
         res = O.true_residual(dx[r].cpu().numpy(), b[r], g, L_SUN, kappa, antiperiodic_t=True)
         assert res < 2 * tol, (n, inner, r, res)
+
+
+@pytest.mark.parametrize("prec", [1, 4])
+def test_slab_site_order_bit_identical(cuda, qcu_lib, prec):
+    """16x16x12x32 SU(3), nrhs 128 (fields of 604 MB FP32, larger than L2):
+    the register kernel walks the lattice in slabs of z-planes (6 by the
+    host's rule here).  The result is bit-identical in the field's own order
+    and in slabs of 3 and 2 planes, and meets the oracle's tolerance (two
+    basis RHS checked, the rest by linearity)."""
+    torch, Q = cuda, qcu_lib
+    L, n, nrhs = (16, 16, 12, 32), 3, 128
+    g = S.random_gauge(L, n, seed=700)
+    got = {}
+    try:
+        for zs in (None, "0", "3", "2"):
+            if zs is None:
+                os.environ.pop("QCU_DSLASH_ZSLAB", None)
+            else:
+                os.environ["QCU_DSLASH_ZSLAB"] = zs
+            errs, outs = linear_check_outputs(torch, Q, g, L, n, prec, nrhs, seed=701)
+            assert max(errs) < TOL[prec], (zs, max(errs))
+            got[zs] = outs
+    finally:
+        os.environ.pop("QCU_DSLASH_ZSLAB", None)
+    for zs in ("0", "3", "2"):
+        assert all(torch.equal(a, b) for a, b in zip(got[None], got[zs])), zs
+
+
+def linear_check_outputs(torch, Q, g, L, n, prec, nrhs, seed):
+    """As linear_check, also returning the output fields (on the device)."""
+    vh = S.half_volume(L)
+    rng = np.random.default_rng(seed)
+    base = (rng.standard_normal((2, vh, 4, n)) + 1j * rng.standard_normal((2, vh, 4, n))) * np.sqrt(0.5)
+    coef = rng.standard_normal((nrhs, 2))
+    ref = O.dslash(base, g, L, 1, 0, True)
+    Q.initGridSize(L, n)
+    Q.set_antiperiodic_t(True)
+    dg = dev(torch, g)
+    Q.loadQcuGauge(dg.data_ptr())
+    del dg
+    Q.getDslash(Q.DSLASH_WILSON, 0.0, n, nrhs, prec)
+    db, dref = dev(torch, base), dev(torch, ref)
+    ins = [float(coef[r, 0]) * db[0] + float(coef[r, 1]) * db[1] for r in range(nrhs)]
+    outs = [torch.zeros_like(x) for x in ins]
+    for r in range(nrhs):
+        Q.pushBackFermions(outs[r].data_ptr(), ins[r].data_ptr())
+    Q.startDslash(1, 0)
+    torch.cuda.synchronize()
+    errs = []
+    for r in range(nrhs):
+        want = float(coef[r, 0]) * dref[0] + float(coef[r, 1]) * dref[1]
+        errs.append(float(torch.linalg.vector_norm(outs[r] - want) / torch.linalg.vector_norm(want)))
+    del ins, db, dref
+    return errs, outs
