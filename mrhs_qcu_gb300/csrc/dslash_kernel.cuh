@@ -716,7 +716,7 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
   uint32_t site, grp;
   A.div_groups.divmod(gid, site, grp);
   if (site >= (uint32_t)A.geo.vh) return;
-  uint32_t rest, xh, y, z, t;
+  uint32_t xh, y, z, t;
   const uint32_t rhs0 = grp * R;
   if (A.mask) {
     bool any = false;
@@ -725,7 +725,7 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
     if (!any) return;
   }
 
-  if (A.zb) {  // s-th site of the slab order
+  if (A.zb) {  // the site-th site of the slab order: (slab, t, z in slab, y, x)
     uint32_t q, r, q2, zz, slab;
     A.div_plane.divmod(site, q, r);
     A.div_zb.divmod(q, q2, zz);
@@ -744,7 +744,6 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
   const uint32_t eo = (y + z + t) & 1u;
   const T f = A.dagger ? (T)-1 : (T)1;
   const uint32_t vh = A.geo.vh;
-  const uint32_t nrhs = A.nrhs;
   const E* __restrict__ in = static_cast<const E*>(A.in);
   const E* __restrict__ gauge = static_cast<const E*>(RC ? A.gauge12 : A.gauge);
   constexpr uint32_t NN = RC ? (N - 1) * N : N * N;  // stored components per link

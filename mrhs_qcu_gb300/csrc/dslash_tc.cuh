@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128)
       // operand buffer b is free once the MMAs of hop q - 2 have completed
       bool ok = true;
       if (q >= 2) ok = tma::mbar_poll(bar0 + 8 * b, ((q >> 1) - 1) & 1u, T.err);
-      const unsigned char* stage_p = nullptr;
+      [[maybe_unused]] const unsigned char* stage_p = nullptr;
       if constexpr (NST > 0) {
         // refill the stage hop q - 1 read (all threads have passed its barrier), then wait for hop q's
         if (tid == 0) {

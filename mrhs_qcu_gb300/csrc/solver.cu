@@ -49,8 +49,6 @@
 namespace qcu {
 namespace {
 
-constexpr int kChunk = 8;  // iterations between host checks
-
 __global__ void cg_alpha_kernel(SolverScalars S, int nrhs) {
   const int r = threadIdx.x;
   if (r >= nrhs) return;
