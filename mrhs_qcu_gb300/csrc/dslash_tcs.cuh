@@ -418,7 +418,12 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
       if (!tcs::wait(tmem_full + 8 * acc, ((uint32_t)it >> 1) & 1u, T.err, abort_flag)) break;
       tc::fence_after();
       const uint32_t lane_addr = tmem + ((lq * 32u) << 16) + acc * 64u;
-      // Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K
+      // Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K;
+      // component k of this lane's output at o + k * step (BF16 halves)
+      const uint32_t o = 2u * (site * sstr + rhs) + ri, step = 2u * cstr;
+      unsigned short* const op = reinterpret_cast<unsigned short*>(out) + o;
+      const unsigned short* const xp = xin ? reinterpret_cast<const unsigned short*>(xin) + o : nullptr;
+      const float sgn = ri ? 1.f : -1.f, bfx = A.bf;
 #pragma unroll
       for (int s = 0; s < 4; s++) {
         uint32_t re_k[8], im_k[8];
@@ -430,16 +435,25 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
           tc::fence_before();
           tma::mbar_arrive(tmem_empty + 8 * acc);
         }
+        float val[N];
 #pragma unroll
         for (int a = 0; a < N; a++) {
           const float other = __shfl_xor_sync(0xffffffffu, __uint_as_float(im_k[a]), 1);
-          const float own = __uint_as_float(re_k[a]);
-          float val = ca * (ri ? own + other : own - other);
-          if (live) {
-            const uint32_t idx = 2u * ((uint32_t)(s * N + a) * cstr + site * sstr + rhs) + ri;
-            if (xin) val = fmaf(A.bf, __bfloat162float(xin[idx]), val);
-            // streaming store: the output is not re-read by this launch
-            __stcs(reinterpret_cast<unsigned short*>(out) + idx, __bfloat16_as_ushort(__float2bfloat16_rn(val)));
+          val[a] = ca * fmaf(sgn, other, __uint_as_float(re_k[a]));  // ca (own -+ other), one rounding each
+        }
+        if (live) {
+          // streaming stores: the output is not re-read by this launch
+          if (xp) {
+#pragma unroll
+            for (int a = 0; a < N; a++) {
+              const uint32_t k = (uint32_t)(s * N + a) * step;
+              const float x = __bfloat162float(__ushort_as_bfloat16(xp[k]));
+              __stcs(op + k, __bfloat16_as_ushort(__float2bfloat16_rn(fmaf(bfx, x, val[a]))));
+            }
+          } else {
+#pragma unroll
+            for (int a = 0; a < N; a++)
+              __stcs(op + (uint32_t)(s * N + a) * step, __bfloat16_as_ushort(__float2bfloat16_rn(val[a])));
           }
         }
       }
