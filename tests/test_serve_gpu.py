@@ -93,3 +93,36 @@ def test_hbm_budget_admission(cuda, qcu_lib):
         srv.submit(0, 0.12, 1e-10, [x.data_ptr() for x in dx], [v.data_ptr() for v in db])
     assert e.value.code == 11
     srv.close()
+
+
+def test_site_major_bf16_inner_lanes(cuda, qcu_lib):
+    """Server lanes with site-major BF16 inner fields (the tensor-core dslash,
+    graph-captured solver chunks): requests of 1-7 RHS on an SU(4) and an
+    SU(3) gauge (slot capacity 8, a multiple of 4) reach their tolerances by
+    the oracle's FP64 true residual."""
+    torch, Q = cuda, qcu_lib
+    gauges = {0: ((4, 4, 4, 8), 4), 1: ((4, 4, 4, 4), 3)}
+    g = {k: S.random_gauge(L, n, seed=560 + k) for k, (L, n) in gauges.items()}
+    dg = {k: dev(torch, g[k]) for k in g}
+    srv = Q.Server(8 << 30, max_slots=8, inner_precision=Q.QCU_BF16_SITE_PRECISION)
+    for k, (L, n) in gauges.items():
+        srv.add_gauge(k, L, n, dg[k].data_ptr(), antiperiodic_t=True)
+    rng = np.random.default_rng(561)
+    jobs = []
+    for i in range(5):
+        gid = i % 2
+        L, n = gauges[gid]
+        nr = int(rng.integers(1, 8))
+        b = S.random_fermions(L, n, nr, seed=570 + i, parities=2)
+        kappa, tol = float(rng.uniform(0.10, 0.12)), [1e-8, 1e-10][i % 2]
+        db, dx = fields(torch, b)
+        jobs.append((srv.submit(gid, kappa, tol, [x.data_ptr() for x in dx], [v.data_ptr() for v in db]),
+                     gid, b, kappa, tol, dx, db))
+    for rid, gid, b, kappa, tol, dx, db in jobs:
+        info = srv.wait(rid)
+        assert info.done and info.status == 0, (rid, info.status)
+        L, _ = gauges[gid]
+        for r in range(b.shape[0]):
+            res = O.true_residual(dx[r].cpu().numpy(), b[r], g[gid], L, kappa, antiperiodic_t=True)
+            assert res < 2 * tol, (rid, r, res)
+    srv.close()
