@@ -417,6 +417,13 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
       const uint32_t acc = (uint32_t)it & 1u;
       if (!tcs::wait(tmem_full + 8 * acc, ((uint32_t)it >> 1) & 1u, T.err, abort_flag)) break;
       tc::fence_after();
+      if (lq * 16u >= (uint32_t)T.rt) {
+        // this warp's 32 accumulator lanes are padding rows (tiles of at most
+        // 32 RHS): nothing to read, release the accumulator for its tile after next
+        tc::fence_before();
+        tma::mbar_arrive(tmem_empty + 8 * acc);
+        continue;
+      }
       const uint32_t lane_addr = tmem + ((lq * 32u) << 16) + acc * 64u;
       // Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K;
       // component k of this lane's output at o + k * step (BF16 halves)
