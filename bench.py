@@ -520,6 +520,7 @@ def headline_error(torch, Q, L, n, nrhs, prec, fout, nout_p, psi_dev, g_dev, che
     first `checked` RHS (the oracle runs on the host cores)."""
     from mrhs_qcu_gb300 import synthetic as S
     from oracle import oracle as O
+    checked = min(checked, nrhs)
     vh = S.half_volume(L)
     dsts = [torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
     Q.unpack_fermions([d.data_ptr() for d in dsts], fout.data_ptr(), nout_p, Q.QCU_SRC_EO_HALF, 0, prec)
