@@ -691,7 +691,10 @@ def multi_lattice_bench(torch, Q, reps=20):
             vh = S.half_volume(L)
             g = S.random_sun_torch(4 * 2 * vh, n, gen).view(4, 2, vh, n * n).permute(0, 1, 3, 2)
             gc = g.to(torch.complex64).contiguous()
-            g12 = gc[:, :, :6, :].permute(0, 1, 3, 2).contiguous()  # [4][2][Vh][6]
+            vp = (vh + 31) // 32 * 32  # two-row links in groups of 32 sites: [4][2][Vp/32][6][32]
+            t12 = torch.zeros((4, 2, 6, vp), dtype=gc.dtype, device=gc.device)
+            t12[..., :vh] = gc[:, :, :6, :]
+            g12 = t12.view(4, 2, 6, vp // 32, 32).permute(0, 1, 3, 2, 4).contiguous()
             fin = torch.randn(4 * n * vh * nrhs * 2, generator=gen, device="cuda", dtype=torch.float32)
             fout = torch.empty_like(fin)
             keep += [gc, g12, fin, fout]

@@ -183,8 +183,10 @@ int qcuNorm2MRHSNoAlloc(double *out, const void *field, int precision, size_t n_
 typedef struct QcuHopSegment_s {
   int lattice[4];              /* X, Y, Z, T of this segment's lattice (X even) */
   const void *gauge;           /* [4][2][N*N][Vh] complex, the coalesced gauge layout, in `precision` */
-  const void *gauge_two_row;   /* SU(3) only: [4][2][Vh][6], the first two rows of every link (six
-                                  contiguous components per link), or NULL */
+  const void *gauge_two_row;   /* SU(3) only: the first two rows of every link in groups of 32
+                                  sites, [4][2][Vp/32][6][32] with Vp = Vh rounded up to a multiple
+                                  of 32 (component k of site s of a (mu, parity) block at
+                                  (s / 32) * 192 + 32 k + s % 32), or NULL */
   const void *in;              /* resident MRHS field [4N][Vh][nrhs] (parity 1 - parity) */
   void *out;                   /* resident MRHS field, output parity; not the same memory as in or x */
   const void *x;               /* optional xpay field (output parity), or NULL */

@@ -184,42 +184,28 @@ __device__ __forceinline__ E ld_link(const char* p) {
     return __ldg(reinterpret_cast<const E*>(p));
 }
 
-// The six components of a two-row link stored contiguously ([8][Vh][6]
-// links: 24 bytes in 16-bit, 48 in FP32, 96 in FP64).  16-bit links are read
-// as three 8-byte words.  FP32 and FP64 links are read one component at a
-// time: with the 128-register budget of the FP32 kernel, three 16-byte loads
-// per link measured 5% slower (17.2 vs 18.1 G site*RHS/s at 32^3x64, nrhs 12)
-// while the 8-byte words gained 4% for BF16.
-template <typename E, bool SMEM>
-__device__ __forceinline__ void ld_link6(const char* p, E (&e)[6]) {
-  if constexpr (sizeof(E) == 4) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const uint2 w = SMEM ? *reinterpret_cast<const uint2*>(p + 8 * k) : __ldg(reinterpret_cast<const uint2*>(p + 8 * k));
-      e[2 * k] = *reinterpret_cast<const E*>(&w.x);
-      e[2 * k + 1] = *reinterpret_cast<const E*>(&w.y);
-    }
-  } else {
-#pragma unroll
-    for (int k = 0; k < 6; k++) e[k] = ld_link<E, SMEM>(p + sizeof(E) * k);
-  }
-}
+// Two-row SU(3) gauge layout: per (mu, parity) block, sites in groups of
+// 32, the six components of a group one after another: component k of site s
+// at (s / 32) * 192 + k * 32 + s % 32 (the half volume padded to a multiple of
+// 32).  A warp's read of one component over 32 consecutive sites is one
+// contiguous run (as in a component-major copy), and a site's eight links lie
+// in eight 1.5 KB blocks (instead of 48 arrays).
+__host__ __device__ constexpr uint32_t two_row_site(uint32_t s) { return (s >> 5) * 192u + (s & 31u); }
+__host__ __device__ constexpr uint32_t two_row_vh(uint32_t vh) { return (vh + 31u) & ~31u; }
 
 // SU(3) link from its first two rows: row 2 = conj(row 0 x row 1), each real
 // part one multiply and three FMAs (the reference's two-row gauge read,
 // include/kernels/storageLoadStore/loadAndStore.cuh:17-27, completed in
-// registers).  Reads the six stored components contiguously at lbase (the
-// [8][Vh][6] two-row gauge).
+// registers).  Loads the six stored components at lbase + k * ls_bytes.
 template <typename S, typename T, bool SMEM = false>
-__device__ __forceinline__ void load_su3_two_row(const char* lbase, C2<T> (&u)[3][3]) {
+__device__ __forceinline__ void load_su3_two_row(const char* lbase, uint32_t ls_bytes, C2<T> (&u)[3][3]) {
   using E = typename S::elem;
-  E e[6];
-  ld_link6<E, SMEM>(lbase, e);
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    const auto v = S::to_c(e[k]);
+    const auto v = S::to_c(ld_link<E, SMEM>(lbase));
     u[k / 3][k % 3].x = (T)v.x;
     u[k / 3][k % 3].y = (T)v.y;
+    lbase += ls_bytes;
   }
 #pragma unroll
   for (int j = 0; j < 3; j++) {
@@ -304,16 +290,16 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
     }
   }
 
-  // colour multiply row by row, then reconstruct; full-link component k at
-  // lbase + k * ls_bytes, two-row links' six components contiguous at lbase
+  // colour multiply row by row, then reconstruct; link component k at
+  // lbase + k * ls_bytes
   const char* lbase = reinterpret_cast<const char*>(gauge + link_off);
-  const uint32_t ls_bytes = vh * (uint32_t)sizeof(E);  // full links; two-row links are contiguous
+  const uint32_t ls_bytes = (RC ? 32u : vh) * (uint32_t)sizeof(E);  // component stride (two-row: groups of 32)
   const T klo0 = s * (T)gsign(MU, u0p), klo1 = s * (T)gsign(MU, u1p);
   // SU(3) two-row links: row 2 = conj(row 0 x row 1), reconstructed in the arithmetic precision
   C2<T> ul[RC ? 3 : 1][RC ? 3 : 1];
   if constexpr (RC) {
     static_assert(N == 3, "link reconstruction is SU(3) only");
-    load_su3_two_row<S, T>(lbase, ul);
+    load_su3_two_row<S, T>(lbase, ls_bytes, ul);
   }
 #pragma unroll
   for (int a = 0; a < N; a++) {
@@ -382,8 +368,8 @@ __device__ __forceinline__ void hop(C2<typename Store<P>::real> (&acc)[4][N][R],
 // Each lane performs exactly the FMA sequence of hop() for its RHS, so the
 // results are bit-identical to it.  The 4N spinor components are loaded in
 // order with a running pointer (64-bit adds instead of wide multiply-adds).
-// A full link's components lie at lbase + k * ls_bytes, a two-row link's six
-// contiguously at lbase (global memory, or shared memory when SMEM).
+// The link's components lie at lbase + k * ls_bytes (global memory, or shared
+// memory when SMEM).
 template <int P, int N, int R, int MU, bool FWD, bool RC, bool SMEM = false>
 __device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4][N][R / 2], const DslashArgs& A,
                                        const typename Store<P>::elem* __restrict__ in, const char* lbase,
@@ -457,7 +443,7 @@ __device__ __forceinline__ void hop_pk(float2 (&re)[4][N][R / 2], float2 (&im)[4
   C2<float> ul[RC ? 3 : 1][RC ? 3 : 1];
   if constexpr (RC) {
     static_assert(N == 3, "link reconstruction is SU(3) only");
-    load_su3_two_row<S, float, SMEM>(lbase, ul);
+    load_su3_two_row<S, float, SMEM>(lbase, ls_bytes, ul);
   }
   const float klo0 = s * (float)gsign(MU, u0p), klo1 = s * (float)gsign(MU, u1p);
 #pragma unroll
@@ -575,7 +561,8 @@ __device__ __forceinline__ void hop_any(HopAcc<typename Store<P>::real, N, R, PK
                                        typename Store<P>::real f) {
   if constexpr (PK)
     hop_pk<P, N, R, MU, FWD, RC>(acc.re, acc.im, A, in, reinterpret_cast<const char*>(gauge + link_off),
-                                 (uint32_t)A.geo.vh * (uint32_t)sizeof(typename Store<P>::elem), nb, rhs0, bc, f);
+                                 (RC ? 32u : (uint32_t)A.geo.vh) * (uint32_t)sizeof(typename Store<P>::elem), nb,
+                                 rhs0, bc, f);
   else
     hop<P, N, R, MU, FWD, RC>(acc.c, A, in, gauge, link_off, nb, rhs0, bc, f);
 }
@@ -752,13 +739,14 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
   hacc.zero();
 
   // link offsets: forward links at (mu, p, site), backward at (mu, 1-p, nb);
-  // full links [8][NN][Vh] (component stride Vh), two-row links [8][Vh][6]
-  // (a link's six components contiguous)
-  constexpr uint32_t LSITE = RC ? NN : 1u;
-  const uint32_t lcs = RC ? 1u : vh;
-  const uint32_t lf = p * NN * vh + site * LSITE;
-  const uint32_t lb = (1u - p) * NN * vh;
-  const uint32_t dmu = 2 * NN * vh;  // one direction's links
+  // full links [8][NN][Vh] (component stride Vh), two-row links in groups of
+  // 32 sites (two_row_site, component stride 32)
+  const uint32_t lvh = RC ? two_row_vh(vh) : vh;
+  const uint32_t lcs = RC ? 32u : vh;
+  auto lsite = [](uint32_t s) { return RC ? two_row_site(s) : s; };
+  const uint32_t lf = p * NN * lvh + lsite(site);
+  const uint32_t lb = (1u - p) * NN * lvh;
+  const uint32_t dmu = 2 * NN * lvh;  // one direction's links
   // FP32 and BF16 storage prefetch every hop's links (below; measured 4-19%
   // faster).  FP64 is bound by its FMA pipe and FP16 (with its norm loads)
   // measured 2-6% slower with the prefetch, so they run the hops without it,
@@ -786,39 +774,39 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
     for (uint32_t k = grp; k < NN; k += A.div_groups.d) {
 #pragma unroll
       for (int h = 0; h < 8; h++)
-        prefetch_l1(gauge + ((h >> 1) * dmu + ((h & 1) ? lb + nbr(h) * LSITE : lf) + k * lcs));
+        prefetch_l1(gauge + ((h >> 1) * dmu + ((h & 1) ? lb + lsite(nbr(h)) : lf) + k * lcs));
     }
     hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nbr(0), rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbr(1) * LSITE, nbr(1), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + lsite(nbr(1)), nbr(1), rhs0, (T)1, f);
     hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nbr(2), rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbr(3) * LSITE, nbr(3), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + lsite(nbr(3)), nbr(3), rhs0, (T)1, f);
     hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nbr(4), rhs0, (T)1, f);
-    hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbr(5) * LSITE, nbr(5), rhs0, (T)1, f);
+    hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + lsite(nbr(5)), nbr(5), rhs0, (T)1, f);
     {  // T, with the optional antiperiodic sign
       const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
       const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
       hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nbr(6), rhs0, bcf, f);
-      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbr(7) * LSITE, nbr(7), rhs0, bcb, f);
+      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + lsite(nbr(7)), nbr(7), rhs0, bcb, f);
     }
   } else {
     {  // X
       const uint32_t nf = (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
       const uint32_t nbk = (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
       hop_any<P, N, R, PK, 0, true, RC>(hacc, A, in, gauge, lf, nf, rhs0, (T)1, f);
-      hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + nbk * LSITE, nbk, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 0, false, RC>(hacc, A, in, gauge, lb + lsite(nbk), nbk, rhs0, (T)1, f);
     }
     {  // Y
       const uint32_t nf = (y == Ly - 1) ? site - (Ly - 1) * hx : site + hx;
       const uint32_t nbk = (y == 0) ? site + (Ly - 1) * hx : site - hx;
       hop_any<P, N, R, PK, 1, true, RC>(hacc, A, in, gauge, dmu + lf, nf, rhs0, (T)1, f);
-      hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + nbk * LSITE, nbk, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 1, false, RC>(hacc, A, in, gauge, dmu + lb + lsite(nbk), nbk, rhs0, (T)1, f);
     }
     {  // Z
       const uint32_t pl = A.geo.plane;
       const uint32_t nf = (z == Lz - 1) ? site - (Lz - 1) * pl : site + pl;
       const uint32_t nbk = (z == 0) ? site + (Lz - 1) * pl : site - pl;
       hop_any<P, N, R, PK, 2, true, RC>(hacc, A, in, gauge, 2 * dmu + lf, nf, rhs0, (T)1, f);
-      hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + nbk * LSITE, nbk, rhs0, (T)1, f);
+      hop_any<P, N, R, PK, 2, false, RC>(hacc, A, in, gauge, 2 * dmu + lb + lsite(nbk), nbk, rhs0, (T)1, f);
     }
     {  // T, with the optional antiperiodic sign
       const uint32_t cb = A.geo.cube;
@@ -828,7 +816,7 @@ __device__ __forceinline__ void wilson_site(const DslashArgs& A, uint32_t gid) {
       const T bcf = (A.antiperiodic_t && top) ? (T)-1 : (T)1;
       const T bcb = (A.antiperiodic_t && bot) ? (T)-1 : (T)1;
       hop_any<P, N, R, PK, 3, true, RC>(hacc, A, in, gauge, 3 * dmu + lf, nf, rhs0, bcf, f);
-      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + nbk * LSITE, nbk, rhs0, bcb, f);
+      hop_any<P, N, R, PK, 3, false, RC>(hacc, A, in, gauge, 3 * dmu + lb + lsite(nbk), nbk, rhs0, bcb, f);
     }
   }
 

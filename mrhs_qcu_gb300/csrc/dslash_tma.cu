@@ -123,11 +123,10 @@ void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int n
   encode(m, ptr, dims, strides, box);
 }
 
-void tma_encode_gauge_rows(CUtensorMap* m, const void* ptr, int ebytes, int vh, int nn, int hx) {
-  const cuuint64_t blk = (cuuint64_t)vh * nn * ebytes;  // one (mu, parity) block, bytes
-  const cuuint64_t dims[3] = {blk / 4, 1, 8};
-  const cuuint64_t strides[2] = {blk, blk};
-  const cuuint32_t box[3] = {(cuuint32_t)(hx * nn * ebytes / 4), 1, 1};
+void tma_encode_gauge_groups(CUtensorMap* m, const void* ptr, int ebytes, int vhp, int hx) {
+  const cuuint64_t dims[3] = {(cuuint64_t)32 * ebytes / 4, 6, (cuuint64_t)8 * vhp / 32};
+  const cuuint64_t strides[2] = {(cuuint64_t)32 * ebytes, (cuuint64_t)6 * 32 * ebytes};
+  const cuuint32_t box[3] = {(cuuint32_t)(hx * ebytes / 4), 6, 1};
   encode(m, ptr, dims, strides, box);
 }
 

@@ -25,8 +25,9 @@ bool wait_timeout_selftest(double limit_s, cudaStream_t st);
 // gauge [8][N*N][Vh] with box {hx, N*N, 1}
 void tma_encode_field(CUtensorMap* m, const void* ptr, int ebytes, int nrhs, int vh, int ncomp, int rcta, int hx);
 void tma_encode_gauge(CUtensorMap* m, const void* ptr, int ebytes, int vh, int nn, int hx);
-// links stored site by site, [8][Vh][nn] (the two-row gauge), box {hx * nn, 1, 1}
-void tma_encode_gauge_rows(CUtensorMap* m, const void* ptr, int ebytes, int vh, int nn, int hx);
+// the two-row gauge in groups of 32 sites, [8][vhp/32][6][32] (vhp: Vh padded
+// to 32), as {32 sites, 6 components, 8 vhp / 32 groups}, box {hx, 6, 1}
+void tma_encode_gauge_groups(CUtensorMap* m, const void* ptr, int ebytes, int vhp, int hx);
 // 16-bit storage scales [Vh][nrhs] float with box {rcta, hx}
 void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rcta, int hx);
 // the MRHS field of a tensor-core operand: [site][spin 4][colour N][RHS] of

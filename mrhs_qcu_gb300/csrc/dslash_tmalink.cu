@@ -15,12 +15,14 @@ bool tmalink_runs(const DslashArgs& A, int R, int ebytes, int nn) {
   // one CTA per row; the instances cap registers at 128, so at most 512 threads per CTA
   const int64_t threads = (int64_t)hx * (A.nrhs / R);
   if (threads < 1 || threads > 512) return false;
-  // TMA: box inner extent a multiple of 16 bytes and at most 256 4-byte elements, 16-byte aligned
-  // rows and strides (full links: inner extent hx complexes; two-row links: 6 hx, contiguous)
-  const int inner = (nn == 6 ? 6 : 1) * hx * ebytes;
+  // TMA: box inner extent (hx complexes) a multiple of 16 bytes and at most 256 4-byte
+  // elements, 16-byte aligned rows and strides; two-row links are read out of groups of 32
+  // sites, so a row must lie within one group
+  const int inner = hx * ebytes;
   if (inner % 16 || inner / 4 > 256 || nn > 256) return false;
+  if (nn == 6 && 32 % hx) return false;
   const void* g = (nn == 6) ? A.gauge12 : A.gauge;
-  if (!g || (uintptr_t)g % 16 || ((int64_t)A.geo.vh * ebytes) % 16) return false;
+  if (!g || (uintptr_t)g % 16 || (nn != 6 && ((int64_t)A.geo.vh * ebytes) % 16)) return false;
   if (tmalink_smem_bytes(nn, hx, ebytes) > 200 * 1024) return false;
   // the register kernel's 32-bit offset limits
   if ((int64_t)4 * 3 * A.geo.vh * A.nrhs >= (1ll << 32)) return false;

@@ -5,8 +5,8 @@
 // links for the whole row lie in one row of the gauge: forward hops at the
 // output row itself, backward hops at the neighbour row (the own row, other
 // parity, for x; the y-1, z-1, t-1 row, wrapped, for the others).  So at CTA
-// start one thread issues eight tensor copies, one box per hop ([NN][hx] for
-// full links, the contiguous [hx][6] run of two-row links), each
+// start one thread issues eight tensor copies, one [NN][hx] box per hop (for
+// two-row links, out of the row's group of 32 sites), each
 // completing on its own mbarrier, and every thread waits only for the hop it
 // is about to compute: the links are read from DRAM once per CTA, shared by
 // all nrhs RHS of the row from shared memory, and never occupy L1 or
@@ -55,11 +55,16 @@ __global__ void __maxnreg__(RegCap<MINB>::regs)
       const uint32_t mu = h >> 1;
       const bool fwd = (h & 1) == 0;
       tma::mbar_expect_tx(bar0 + 8 * h, hop_bytes);
-      // full links: box {hx sites, NN components, 1} at (row start, 0, 2 mu + parity); two-row
-      // links: box {6 hx components, 1, 1} at (6 x row start, 0, 2 mu + parity); x in 4-byte units
-      tma::load_3d(tma::smem_u32(smem + h * hop_stride), &gmap,
-                   (int)((fwd ? row : back_row[mu]) * hx * (RC ? 6u : 1u) * (sizeof(E) / 4)), 0,
-                   (int)(2 * mu + (fwd ? p : 1u - p)), bar0 + 8 * h);
+      // box {hx sites, NN components, 1}, x in 4-byte units: full links at (row start, 0,
+      // 2 mu + parity); two-row links at (row start within its group of 32 sites, 0, group
+      // index over all (mu, parity) blocks)
+      const uint32_t lrow = fwd ? row : back_row[mu], blk = 2 * mu + (fwd ? p : 1u - p);
+      if constexpr (RC)
+        tma::load_3d(tma::smem_u32(smem + h * hop_stride), &gmap, (int)(((lrow * hx) & 31u) * (sizeof(E) / 4)), 0,
+                     (int)(blk * (two_row_vh(A.geo.vh) >> 5) + ((lrow * hx) >> 5)), bar0 + 8 * h);
+      else
+        tma::load_3d(tma::smem_u32(smem + h * hop_stride), &gmap, (int)(lrow * hx * (sizeof(E) / 4)), 0, (int)blk,
+                     bar0 + 8 * h);
     }
   }
   // after a timeout anywhere in the launch, later CTAs wait 10 ms instead of
@@ -102,8 +107,8 @@ __global__ void __maxnreg__(RegCap<MINB>::regs)
                           top ? site - (Lt - 1) * cb : site + cb,
                           bot ? site + (Lt - 1) * cb : site - cb};
   // the backward x link is at the x-neighbour in the own row; every other link at the thread's xh
-  // (byte offsets in the staged row: component stride hx for full links, six contiguous for two-row)
-  constexpr uint32_t LB = RC ? 6u * (uint32_t)sizeof(E) : (uint32_t)sizeof(E);
+  // (byte offsets in the staged [NN][hx] row)
+  constexpr uint32_t LB = (uint32_t)sizeof(E);
   const uint32_t lx[8] = {xh * LB, (nbx_b - row * hx) * LB, xh * LB, xh * LB, xh * LB, xh * LB, xh * LB, xh * LB};
   const uint32_t ls_bytes = hx * (uint32_t)sizeof(E);
   const float bcf = (A.antiperiodic_t && top) ? -1.f : 1.f;
@@ -158,7 +163,7 @@ void launch_wilson_tmalink(const DslashArgs& A, int /*block*/, cudaStream_t st) 
               "link-staged dslash: arguments outside the kernel's limits");
   CUtensorMap mg;
   if constexpr (RC)
-    tma_encode_gauge_rows(&mg, A.gauge12, (int)sizeof(E), A.geo.vh, 6, A.geo.hx);
+    tma_encode_gauge_groups(&mg, A.gauge12, (int)sizeof(E), (int)detail::two_row_vh(A.geo.vh), A.geo.hx);
   else
     tma_encode_gauge(&mg, A.gauge, (int)sizeof(E), A.geo.vh, NN, A.geo.hx);
   const size_t smem = tmalink_smem_bytes(NN, A.geo.hx, (int)sizeof(E));

@@ -215,7 +215,9 @@ __global__ void compress_gauge_kernel(const double2* __restrict__ src, void* dst
     } else {
       e = S::from_c(make_float2((float)v.x, (float)v.y));
     }
-    static_cast<E*>(dst)[blk * 6 * vh + site * 6 + comp] = e;  // [8][Vh][6]: one link's six contiguous
+    // [8][Vh/32][6][32] (Vh padded to 32): the groups of 32 sites of dslash_kernel.cuh two_row_site
+    const int64_t vhp = (vh + 31) / 32 * 32;
+    static_cast<E*>(dst)[blk * 6 * vhp + (site >> 5) * 192 + comp * 32 + (site & 31)] = e;
   }
 }
 

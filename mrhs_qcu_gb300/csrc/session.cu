@@ -341,7 +341,8 @@ const void* Session::gauge12(int prec) {
   const double tol = prec == PREC_DOUBLE ? 1e-13 : (prec == PREC_SINGLE ? 1e-7 : 1e-4);
   if (!(su3_dev_ < tol)) return nullptr;
   if (!gauge12_valid_[prec]) {
-    void* d = gauge12_[prec].ensure((size_t)48 * geo.vh * prec_complex_bytes(prec));
+    const size_t vhp = ((size_t)geo.vh + 31) / 32 * 32;  // the two-row layout's groups of 32 sites
+    void* d = gauge12_[prec].ensure(48 * vhp * prec_complex_bytes(prec));
     compress_gauge_su3(gauge_[PREC_DOUBLE].get(), prec, d, geo.vh, stream());
     gauge12_valid_[prec] = true;
   }

@@ -117,17 +117,16 @@ def _pin(R, minb, pk, rc, lt, block=64):
 
 
 @pytest.mark.parametrize("prec,rc,L,nrhs", [
-    (1, 1, (4, 4, 4, 8), 12), (1, 0, (4, 4, 4, 8), 2), (1, 1, (12, 4, 6, 4), 12), (1, 1, (16, 6, 4, 10), 64),
+    (1, 1, (4, 4, 4, 8), 12), (1, 0, (4, 4, 4, 8), 2), (1, 0, (12, 4, 6, 4), 12), (1, 1, (16, 6, 4, 10), 64),
     (1, 0, (8, 8, 8, 16), 24), (1, 1, (8, 8, 8, 16), 4), (4, 1, (8, 8, 8, 16), 12), (4, 1, (16, 6, 4, 10), 64),
-    (1, 1, (6, 4, 4, 4), 12), (4, 1, (4, 4, 4, 8), 4)])
+    (1, 1, (32, 4, 2, 4), 12), (4, 1, (8, 4, 4, 4), 4)])
 def test_link_staged_kernel(cuda, qcu_lib, prec, rc, L, nrhs):
     """The register kernel with its links staged by TMA into shared memory
     (one CTA per x-row, eight boxes on eight mbarriers): against the oracle on
-    both parities, dagger flags and antiperiodic t, for rows of 2..8 sites
-    (3 with two-row FP32 links, whose contiguous row is 144 bytes), 1..32 RHS
-    groups, full and two-row links, FP32 and BF16 storage; launched (not a
-    fallback) and bit-identical to the register kernel of the same R and
-    link form."""
+    both parities, dagger flags and antiperiodic t, for rows of 2..16 sites,
+    1..32 RHS groups, full and two-row links, FP32 and BF16 storage; launched
+    (not a fallback) and bit-identical to the register kernel of the same R
+    and link form."""
     Q = qcu_lib
     g = S.random_gauge(L, 3, seed=600 + nrhs)
     psi = S.random_fermions(L, 3, nrhs, seed=601 + nrhs)
@@ -147,13 +146,14 @@ def test_link_staged_kernel(cuda, qcu_lib, prec, rc, L, nrhs):
         os.environ.pop("QCU_DSLASH_CONFIG", None)
 
 
-@pytest.mark.parametrize("L,prec,rc", [((6, 4, 4, 4), 1, 0), ((6, 4, 4, 4), 4, 1), ((10, 4, 2, 4), 4, 1)])
+@pytest.mark.parametrize("L,prec,rc", [((6, 4, 4, 4), 1, 0), ((6, 4, 4, 4), 4, 1), ((10, 4, 2, 4), 4, 1),
+                                       ((12, 4, 6, 4), 1, 1)])
 def test_link_staged_kernel_falls_back(cuda, qcu_lib, L, prec, rc):
-    """A row whose links are not a whole number of 16-byte units cannot be a
-    TMA box: full FP32 links of X/2 = 3 sites (24 bytes per component row),
-    two-row BF16 links of 3 or 5 sites (72 or 120 contiguous bytes).  The
-    pinned link-staged shape runs the register kernel, with the oracle's
-    result."""
+    """Rows the link-staged kernel cannot copy as a TMA box: component rows
+    that are not a whole number of 16-byte units (X/2 = 3 FP32 sites, 24
+    bytes; 3 or 5 BF16 sites), and two-row links of rows that do not divide
+    the gauge's groups of 32 sites (X/2 = 6).  The pinned link-staged shape
+    runs the register kernel, with the oracle's result."""
     Q = qcu_lib
     g = S.random_gauge(L, 3, seed=610)
     psi = S.random_fermions(L, 3, 4, seed=611)

@@ -20,11 +20,14 @@ LATTICES = [((8, 8, 8, 8), 12), ((4, 4, 4, 8), 4), ((8, 4, 6, 4), 6), ((4, 6, 4,
 
 def coalesced_gauge(torch, g, prec):
     """[4][2][Vh][3][3] complex128 caller gauge -> the coalesced [4][2][9][Vh] layout in `prec`, and the
-    two-row copy [4][2][Vh][6] (each link's first two rows contiguous)"""
+    two-row copy in groups of 32 sites, [4][2][Vp/32][6][32] (Vp = Vh padded to 32)"""
     vh = g.shape[2]
     c = torch.from_numpy(np.ascontiguousarray(g.reshape(4, 2, vh, 9).transpose(0, 1, 3, 2))).cuda()
     c = c.to(torch.complex64 if prec == 1 else torch.complex128).contiguous()
-    return c, c[:, :, :6, :].permute(0, 1, 3, 2).contiguous()
+    vp = (vh + 31) // 32 * 32
+    t = torch.zeros((4, 2, 6, vp), dtype=c.dtype, device=c.device)
+    t[..., :vh] = c[:, :, :6, :]
+    return c, t.view(4, 2, 6, vp // 32, 32).permute(0, 1, 3, 2, 4).contiguous()
 
 
 @pytest.mark.parametrize("prec,pin", [(1, "2,64,2,1,0,0,0,1"), (1, "2,128,2,0,0,0,0,0"), (2, "1,64,1,0,0,0,0,1")])
