@@ -127,6 +127,9 @@ void plan_site_order(DslashArgs& B, int prec, int N) {
     while (d > 1 && g.L[2] % d) d--;  // the next smaller divisor of Lz
     zb = d;
   }
+  // slabs thinner than 4 planes re-read more of their z faces than the field
+  // order loses to L2 (2 / zb of the input per launch)
+  if (zb < 4) zb = g.L[2];
   // QCU_DSLASH_ZSLAB=<planes> overrides the choice (0: the field's order)
   if (const char* e = getenv("QCU_DSLASH_ZSLAB")) {
     const int v = atoi(e);
