@@ -94,6 +94,45 @@ __global__ void unpack_fermions_kernel(PtrArray dstp, int mode, int parity, cons
   }
 }
 
+// Unpack through a shared-memory tile (caller layouts whose sites are
+// contiguous: one parity or both parities in eo order).  A block stages ts
+// sites x tr RHS of the MRHS field as FP64 complex: the reads walk the
+// field's contiguous (site, RHS) runs of each component, the writes each
+// RHS's contiguous run of ts sites x 4N caller components.  (One thread per
+// (site, RHS) scatters every warp's writes over up to 32 RHS arrays.)
+template <int P, int N>
+__global__ void unpack_fermions_tiled_kernel(PtrArray dstp, int mode, int parity, const void* src,
+                                             const float* src_norm, Geometry g, int nrhs, int ts, int tr) {
+  using S = Store<P>;
+  using E = typename S::elem;
+  constexpr int NC = 4 * N;
+  extern __shared__ double2 tile[];  // [tr][ts][NC]
+  const int64_t site0 = (int64_t)blockIdx.x * ts;
+  const int r0 = blockIdx.y * tr;
+  const int64_t cs = field_comp_stride(P, g.vh, NC, nrhs), ss = field_site_stride(P, g.vh, NC, nrhs);
+  const E* in = static_cast<const E*>(src);
+  const int n = NC * ts * tr;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int r = i % tr, s = (i / tr) % ts, c = i / (tr * ts);
+    const int64_t site = site0 + s;
+    const int rhs = r0 + r;
+    if (site >= g.vh || rhs >= nrhs) continue;
+    const auto v = S::to_c(in[site * ss + c * cs + rhs]);
+    double scale = 1.0;
+    if constexpr (S::has_norm) scale = (double)src_norm[site * nrhs + rhs];
+    tile[((int64_t)r * ts + s) * NC + c] = make_double2((double)v.x * scale, (double)v.y * scale);
+  }
+  __syncthreads();
+  const int64_t base = (mode == SRC_EO_FULL ? (int64_t)parity * g.vh : 0) + site0;  // caller site of site0
+  const int nsites = (int)min((int64_t)ts, g.vh - site0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int r = i / (ts * NC), rem = i - r * ts * NC;
+    const int rhs = r0 + r;
+    if (rem >= nsites * NC || rhs >= nrhs || dstp.p[rhs] == nullptr) continue;  // a null pointer skips RHS r
+    static_cast<double2*>(const_cast<void*>(dstp.p[rhs]))[base * NC + rem] = tile[(int64_t)r * ts * NC + rem];
+  }
+}
+
 // gauge: caller (eo or lexicographic) complex double -> [4][2][N*N][Vh] P
 template <int P>
 __global__ void pack_gauge_kernel(const double2* __restrict__ src, int lex, void* dst, Geometry g, int nn) {
@@ -279,6 +318,24 @@ void pack_n(int prec, const PtrArray& src, int mode, int parity, void* dst, floa
 template <int N>
 void unpack_n(int prec, const PtrArray& dst, int mode, int parity, const void* src, const float* src_norm,
               const Geometry& g, int nrhs, cudaStream_t st) {
+  if (mode != SRC_LEX) {
+    // tiles of ts sites x tr RHS, 48 KB of FP64 complex in shared memory
+    const int tr = std::min(nrhs, 16);
+    const int ts = std::max(1, std::min(32, 3072 / (tr * 4 * N)));
+    const dim3 grid((unsigned)((g.vh + ts - 1) / ts), (unsigned)((nrhs + tr - 1) / tr));
+    const size_t smem = (size_t)ts * tr * 4 * N * sizeof(double2);
+#define QCU_UNPACK_TILED(PR)                                                                                      \
+  unpack_fermions_tiled_kernel<PR, N><<<grid, 256, smem, st>>>(dst, mode, parity, src, src_norm, g, nrhs, ts, tr); \
+  return;
+    switch (prec) {
+      case PREC_DOUBLE: QCU_UNPACK_TILED(PREC_DOUBLE)
+      case PREC_SINGLE: QCU_UNPACK_TILED(PREC_SINGLE)
+      case PREC_HALF: QCU_UNPACK_TILED(PREC_HALF)
+      case PREC_BF16: QCU_UNPACK_TILED(PREC_BF16)
+      case PREC_BF16S: QCU_UNPACK_TILED(PREC_BF16S)
+    }
+#undef QCU_UNPACK_TILED
+  }
   const int64_t threads = (int64_t)g.vh * nrhs;
   const int block = 128;
   const int grid = (int)((threads + block - 1) / block);
