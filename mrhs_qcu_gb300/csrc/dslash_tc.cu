@@ -115,14 +115,17 @@ int tc_grid(const void* kernel, int ntiles, size_t smem, int tmem_cols, int thre
   return std::min(ntiles, occ * sms);
 }
 
+// one key per (precision, N <= 15, variant <= 15)
+static int tc_key(int prec, int N, int variant) { return (prec * 16 + N) * 16 + variant; }
+
 void register_tc(int prec, int N, int variant, TcLauncher fn) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  registry()[(prec * 16 + N) * 8 + variant] = fn;
+  registry()[tc_key(prec, N, variant)] = fn;
 }
 
 TcLauncher find_tc(int prec, int N, int variant) {
   std::lock_guard<std::mutex> lk(registry_mutex());
-  auto it = registry().find((prec * 16 + N) * 8 + variant);
+  auto it = registry().find(tc_key(prec, N, variant));
   return it == registry().end() ? nullptr : it->second;
 }
 

@@ -83,7 +83,7 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
 // half-spinor operands, dslash_tc.cuh); 4 / 5 / 6 = the spinor-operand kernel
 // (dslash_tcs.cuh) with (TMA stages, B buffers) = (4, 3) / (6, 3) / (3, 2);
 // 7 / 8 = the same with one 32-RHS half per stage, (8, 3) / (6, 4)
-constexpr int kTcVariants = 8;
+constexpr int kTcVariants = 8;  // <= 15 (registry keys)
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
 void register_tc(int prec, int N, int variant, TcLauncher fn);
 TcLauncher find_tc(int prec, int N, int variant = 1);
