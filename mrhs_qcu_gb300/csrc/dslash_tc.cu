@@ -70,7 +70,9 @@ bool tcs_plan(const DslashArgs& A, int N, TcsDslashArgs* T, CUtensorMap* map_in)
   while (nrhs % rt || rt % 4) rt--;
   const int64_t ntiles = (int64_t)geo.vh * (nrhs / rt);
   if (ntiles >= (1ll << 31)) return false;
-  if (!tma_encode_field_swizzled(map_in, A.in, nrhs, geo.vh, N, A.site_major != 0)) return false;
+  // tiles of 64 RHS: one copy per hop brings both halves (5-D map), else one per half
+  T->fused = rt == 64 && tma_encode_field_swizzled_halves(map_in, A.in, nrhs, geo.vh, N, A.site_major != 0);
+  if (!T->fused && !tma_encode_field_swizzled(map_in, A.in, nrhs, geo.vh, N, A.site_major != 0)) return false;
   T->cstr = (uint32_t)(A.site_major ? nrhs : geo.vh * nrhs);
   T->sstr = (uint32_t)(A.site_major ? 4 * N * nrhs : nrhs);
   T->rt = rt;

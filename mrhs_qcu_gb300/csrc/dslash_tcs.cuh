@@ -30,14 +30,15 @@
 // each other through mbarriers only:
 //   warps 0-3  B builders: per hop, the 4 KB B operand into a ring of NB
 //              buffers, each thread two 16-byte chunks: signed copies of one
-//              link row that arrived with the A block
+//              link row of the tile's link record
 //   warp 4     MMA issuer (one thread): two MMAs per hop into one of two
 //              tensor-memory accumulators; commits free the B buffer and the
 //              TMA stage, and hand a finished tile to the epilogue
 //   warp 5     TMA producer (one thread): per hop, the neighbour's A block
-//              (one or two boxes of 32 RHS) and the link in row form (one
-//              256-byte bulk copy, layout.h gauge_tc_rows_bf16) into a ring
-//              of NST stages, as far ahead as the ring allows
+//              (one box, or two of 32 RHS) into a ring of NST stages, as far
+//              ahead as the ring allows; per tile, with its first hop, the
+//              site's link record (one 2 KB bulk copy, layout.h
+//              gauge_tc_records_bf16) into one of two record slots
 //   warps 6-9  epilogue: tensor memory -> Re/Im combination -> global, one
 //              tile behind the MMAs (double-buffered accumulator)
 // Every wait is bounded (about 1 s); a timeout sets *err and a shared abort
@@ -57,7 +58,8 @@ struct TcsDslashArgs {
   int rt;      // RHS per tile (<= 64)
   int chunks;  // nrhs / rt
   int ntiles;  // vh * chunks
-  int halves;  // A boxes of 32 RHS per tile: 1 (rt <= 32) or 2
+  int halves;  // A halves of 32 RHS per tile: 1 (rt <= 32) or 2
+  int fused;   // 1: the tensor map is 5-D and one box brings both halves (nrhs a multiple of 32)
   int* err;    // set to 1 when a wait times out
   // complex-element strides of the output and xpay fields between components
   // and between sites (component- or site-major layout)
@@ -67,28 +69,37 @@ struct TcsDslashArgs {
 namespace tcs {
 
 constexpr uint32_t kHalfBytes = 4096;               // 4 spins x 8 colours x 128 B (32 RHS)
-constexpr uint32_t kLinkBytes = 1024;               // one link in row form (256 B), 1 KB keeps stages aligned
+constexpr uint32_t kRecBytes = 2048;                // a site's eight links in row form (layout.h kTcRecordBytes)
 constexpr uint32_t kBBytes = 4096;                  // 64 (n) x 32 (k) BF16, K-major
 constexpr uint32_t kTmemCols = 128;  // two accumulators of 64 columns
-// A stage holds HV A halves of 32 RHS (M rows 64 h .. 64 h + 63) and the
-// link.  With HV = 1 (tiles of at most 32 RHS) the MMA's rows 64-127 read
-// the 4 KB after the half, whatever lies there: their accumulator lanes are
-// never stored, and the read stays inside the CTA's shared memory (the B
-// buffers follow the last stage).
-__host__ __device__ constexpr uint32_t stage_bytes(int hv) { return (uint32_t)hv * kHalfBytes + kLinkBytes; }
+// A stage holds HV A halves of 32 RHS (M rows 64 h .. 64 h + 63).  With
+// HV = 1 (tiles of at most 32 RHS) the MMA's rows 64-127 read the 4 KB after
+// the half, whatever lies there: their accumulator lanes are never stored,
+// and the read stays inside the CTA's shared memory (the link records and
+// the B buffers follow the last stage).
+__host__ __device__ constexpr uint32_t stage_bytes(int hv) { return (uint32_t)hv * kHalfBytes; }
 
+// Link records: tile k of a CTA uses slot k % 3, fetched during tile k - 1.
+// Slot k % 3 was last read in tile k - 3, which the builders have finished
+// when the producer, at the first hop of tile k - 1, has seen the MMAs of a
+// hop of tile k - 2 complete (rings of at most 8 stages).
+constexpr int kRecSlots = 3;
 // offsets from the 1024-byte aligned base of dynamic shared memory: TMA
-// stages, B buffers, barriers
-__host__ __device__ constexpr uint32_t b_off(int nst, int hv) { return (uint32_t)nst * stage_bytes(hv); }
+// stages, link records, B buffers, barriers
+__host__ __device__ constexpr uint32_t rec_off(int nst, int hv) { return (uint32_t)nst * stage_bytes(hv); }
+__host__ __device__ constexpr uint32_t b_off(int nst, int hv) { return rec_off(nst, hv) + kRecSlots * kRecBytes; }
 __host__ __device__ constexpr uint32_t bar_off(int nst, int nb, int hv) { return b_off(nst, hv) + (uint32_t)nb * kBBytes; }
 // barriers: ring_full[nst], ring_empty[nst], b_full[nb], b_empty[nb],
-// tmem_full[2], tmem_empty[2], drain; then the tensor-memory slot and the abort flag
+// tmem_full[2], tmem_empty[2], drain, rec_full[3]; then the tensor-memory slot and the abort flag
 __host__ __device__ constexpr uint32_t slot_off(int nst, int nb, int hv) {
-  return bar_off(nst, nb, hv) + 8u * (2 * nst + 2 * nb + 5);
+  return bar_off(nst, nb, hv) + 8u * (2 * nst + 2 * nb + 5 + kRecSlots);
 }
 // + 1024 bytes to align the base
 __host__ __device__ constexpr uint32_t smem_bytes(int nst, int nb, int hv) { return slot_off(nst, nb, hv) + 16 + 1024; }
 constexpr int kThreads = 320;
+// epilogue warps with accumulator rows to store: warp w holds rows 32 w .. 32 w + 31,
+// RHS 16 w .. 16 w + 15 of the tile; the others leave at once
+__host__ __device__ constexpr uint32_t epilogue_warps(int rt) { return (uint32_t)(rt + 15) / 16u; }
 
 // instruction descriptor, kind::f16: D = F32, A = B = BF16, A MN-major (bit
 // 15), B K-major, N = 64, M = 128
@@ -117,38 +128,22 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-// coordinates of an output site, decomposed once per tile
-struct SiteCoords {
-  uint32_t site, xh, y, z, t, eo;
-  __device__ __forceinline__ SiteCoords(const DslashArgs& A, uint32_t s) : site(s) {
-    uint32_t rest, rest2;
-    A.geo.div_hx.divmod(s, rest, xh);
-    A.geo.div_y.divmod(rest, rest2, y);
-    A.geo.div_z.divmod(rest2, t, z);
-    eo = (y + z + t) & 1u;
-  }
-  // neighbour for hop d = 2 mu + (backward ? 1 : 0) (d known at compile time)
-  __device__ __forceinline__ uint32_t nb(const DslashArgs& A, int d) const {
-    const uint32_t hx = A.geo.hx, p = A.parity;
-    switch (d) {
-      case 0: return (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
-      case 1: return (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
-      case 2: return (y == A.geo.L[1] - 1) ? site - (A.geo.L[1] - 1) * hx : site + hx;
-      case 3: return (y == 0) ? site + (A.geo.L[1] - 1) * hx : site - hx;
-      case 4: return (z == A.geo.L[2] - 1) ? site - (A.geo.L[2] - 1) * A.geo.plane : site + A.geo.plane;
-      case 5: return (z == 0) ? site + (A.geo.L[2] - 1) * A.geo.plane : site - A.geo.plane;
-      case 6: return (t == A.geo.L[3] - 1) ? site - (A.geo.L[3] - 1) * A.geo.cube : site + A.geo.cube;
-      default: return (t == 0) ? site + (A.geo.L[3] - 1) * A.geo.cube : site - A.geo.cube;
-    }
-  }
-};
-
 // L2 policy that keeps lines resident (each neighbour block is read by the
 // eight sites around it, a short while apart)
 __device__ __forceinline__ uint64_t evict_last_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
   return pol;
+}
+
+// 5-D tiled TMA load into shared memory with an L2 cache policy, completion counted on bar
+__device__ __forceinline__ void load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                        uint32_t bar, uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, "
+      "{%2, %3, %4, %5, %6}], [%7], %8;" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar), "l"(policy)
+      : "memory");
 }
 
 // 4-D tiled TMA load into shared memory with an L2 cache policy, completion counted on bar
@@ -190,22 +185,53 @@ __device__ __forceinline__ bool wait(uint32_t bar, uint32_t parity, int* err, vo
   }
 }
 
+// The same bounded wait for roles off the critical path: the epilogue waits
+// a whole tile for its accumulator and the producer runs a ring ahead of the
+// MMAs.  Between polls the warp sleeps (64 ns doubling to 1 us), so it takes
+// no issue slots from the builders and the MMA issuer, which poll.
+__device__ __forceinline__ bool wait_sleep(uint32_t bar, uint32_t parity, int* err, volatile int* abort_flag) {
+  uint32_t ok = 0;
+  const uint64_t t0 = tma::now_ns();
+  uint32_t ns = 64;
+  for (uint32_t i = 1;; i++) {
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*abort_flag) return false;
+    __nanosleep(ns);
+    ns = ns < 1024u ? 2u * ns : 1024u;
+    if ((i & 15u) == 0 && tma::now_ns() - t0 > 1000000000ull) {
+      atomicExch(err, 1);
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+
 }  // namespace tcs
 
 // map_in: the input field as [site][spin 4][colour N][RHS] of 4-byte complex
 // BF16 (strides of either layout), box (32 RHS, 8 colours, 4 spins, 1 site),
-// 128-byte swizzle.  In the site-major layout a box is one contiguous 4 KB
-// run of the field; in the component-major one it gathers 32 rows of 128
-// bytes from arrays Vh x nrhs x 4 bytes apart, which the copy engine serves
-// at about half the rate when a hop's block is 8 KB.  The
-// links come from A.gauge_tc (BF16 row form, one 256-byte bulk copy per hop).
+// 128-byte swizzle; or, when the RHS count is a multiple of 32 and a tile
+// holds 64 RHS (T.fused), as [site][half][spin][colour][RHS 32] with box
+// (32, 8, 4, 2, 1), which lands a tile's two halves in one copy.  The copy
+// engine's cost per copy hardly depends on its size, and with 4 CTAs per SM
+// the producer spends most of each hop waiting to issue, so the copies per
+// site are what count.  In the site-major layout a box is one contiguous run
+// of the field; in the component-major one it gathers rows of 128 bytes from
+// arrays Vh x nrhs x 4 bytes apart, which the copy engine serves at about
+// half the rate.  The links come from A.gauge_tc: one 2 KB record per site
+// (its eight links in row form), one bulk copy per tile.
 template <int N, int NST, int NB, int HV>
 __global__ void __launch_bounds__(tcs::kThreads, 4)
     wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
   static_assert(N >= 2 && N <= 8, "colours are padded to 8");
   static_assert(NST >= 2 && NST <= 8 && NB >= 2 && NB <= 4, "ring depths");
   static_assert(HV == 1 || HV == 2, "A halves per stage");
-  constexpr uint32_t kStage = tcs::stage_bytes(HV), kA = (uint32_t)HV * tcs::kHalfBytes;
+  constexpr uint32_t kStage = tcs::stage_bytes(HV);
   using namespace detail;
   const DslashArgs& A = T.A;
   extern __shared__ unsigned char smem_raw[];
@@ -220,6 +246,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
   const uint32_t tmem_full = b_empty + 8 * NB;
   const uint32_t tmem_empty = tmem_full + 16;
   const uint32_t drain = tmem_empty + 16;
+  const uint32_t rec_full = drain + 8;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + tcs::slot_off(NST, NB, HV));
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + tcs::slot_off(NST, NB, HV) + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -235,9 +262,10 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     }
     for (int i = 0; i < 2; i++) {
       tma::mbar_init(tmem_full + 8 * i, 1);
-      tma::mbar_init(tmem_empty + 8 * i, 128);
+      tma::mbar_init(tmem_empty + 8 * i, 32 * tcs::epilogue_warps(T.rt));
     }
     tma::mbar_init(drain, 1);
+    for (int i = 0; i < tcs::kRecSlots; i++) tma::mbar_init(rec_full + 8 * i, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -264,20 +292,23 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     const bool dag = A.dagger != 0;
     uint32_t q = 0;
     bool stop = false;
-    for (int tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x) {
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !stop; tile += gridDim.x, it++) {
       const uint32_t site = (uint32_t)(tile / T.chunks);
-      const uint32_t t_coord = tcs::SiteCoords(A, site).t;
+      const uint32_t t_coord = EoSite(A.geo, site).t;
       auto hop = [&](auto dc) -> bool {
         constexpr int D = decltype(dc)::value;
         constexpr int mu = D >> 1;
         constexpr bool fwd = (D & 1) == 0;
         constexpr bool imag = gimag(mu);
-        const uint32_t st = q % NST, b = q % NB;
+        const uint32_t b = q % NB;
         // B buffer b is free once the MMAs of hop q - NB have completed; the
-        // hop's link rows arrive with its A block
+        // tile's link record is in place before its first hop is built.  The
+        // builders never read the A stage, so the build of a hop overlaps the
+        // copy of its neighbour block (the MMA issuer waits for both).
         bool ok = true;
         if (q >= NB) ok = tcs::wait(b_empty + 8 * b, ((q / NB) - 1) & 1u, T.err, abort_flag);
-        if (ok) ok = tcs::wait(ring_full + 8 * st, (q / NST) & 1u, T.err, abort_flag);
+        if (D == 0 && ok) ok = tcs::wait(rec_full + 8 * (it % tcs::kRecSlots), (it / tcs::kRecSlots) & 1u, T.err, abort_flag);
         if (!ok) return false;
         // stage 2: K_hop chunk for output spin s = cs_, input spin g = cg, colour a = ca_:
         // z = P[s][g] = bc (g = s) or bc * sg * (i if imag) (g = perm(s)) or 0
@@ -295,9 +326,11 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
         const bool diag = cg == cs_, off = cg == perm;
         const float sg = (diag ? 1.f : (fwd ? -1.f : 1.f) * (float)gs * (dag ? -1.f : 1.f)) * bc;
         const bool zim = off && imag;
-        // link rows in the stage: row (part, a) of W = U (forward) or of U^T
-        // (backward, whose conjugation flips the sign of the Im part)
-        const unsigned char* wr = smem + st * kStage + kA;
+        // the hop's link in the tile's record (which arrived with hop 0): row
+        // (part, a) of W = U (forward) or of U^T (backward, whose conjugation
+        // flips the sign of the Im part)
+        const unsigned char* wr =
+            smem + tcs::rec_off(NST, HV) + (uint32_t)(it % tcs::kRecSlots) * tcs::kRecBytes + D * 256u;
         unsigned char* bbuf = smem + tcs::b_off(NST, HV) + b * tcs::kBBytes;
 #pragma unroll
         for (int part = 0; part < 2; part++) {
@@ -363,34 +396,50 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     // ---- TMA producer --------------------------------------------------------
     if (lane == 0) {
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_in)) : "memory");
-      constexpr uint32_t kLink = 256;  // layout.h kTcLinkBytes
       const unsigned char* gtc = static_cast<const unsigned char*>(A.gauge_tc);
       const uint32_t vh = A.geo.vh;
-      const uint32_t tx = (uint32_t)T.halves * tcs::kHalfBytes + kLink;
+      const uint32_t tx = (uint32_t)T.halves * tcs::kHalfBytes;
       const uint64_t keep = tcs::evict_last_policy();
       uint32_t qq = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      int it = 0;
+      // link record of tile `it` (its site's eight links, 2 KB) into slot it % 3
+      auto fetch_record = [&](int tile_r, int it_r) {
+        const uint32_t bar = rec_full + 8 * (it_r % tcs::kRecSlots);
+        tma::mbar_expect_tx(bar, tcs::kRecBytes);
+        tcs::bulk_load(smem0 + tcs::rec_off(NST, HV) + (uint32_t)(it_r % tcs::kRecSlots) * tcs::kRecBytes,
+                       gtc + ((uint64_t)p * vh + (uint32_t)(tile_r / T.chunks)) * tcs::kRecBytes, tcs::kRecBytes, bar);
+      };
+      int fetched = 0;  // records issued
+      if ((int)blockIdx.x < ntiles) {
+        fetch_record(blockIdx.x, 0);
+        fetched = 1;
+      }
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
         const uint32_t st_site = (uint32_t)(tile / T.chunks), st_chunk = (uint32_t)(tile % T.chunks);
-        const tcs::SiteCoords sc(A, st_site);
+        const EoSite sc(A.geo, st_site);
 #pragma unroll
         for (int d = 0; d < 8; d++, qq++) {
           const uint32_t st = qq % NST;
           // stage st is free once the MMAs of hop qq - NST have completed
-          if (qq >= (uint32_t)NST && !tcs::wait(ring_empty + 8 * st, ((qq / NST) - 1) & 1u, T.err, abort_flag)) {
+          if (qq >= (uint32_t)NST && !tcs::wait_sleep(ring_empty + 8 * st, ((qq / NST) - 1) & 1u, T.err, abort_flag)) {
             ok = false;
             break;
           }
-          const uint32_t nbq = sc.nb(A, d);
-          const uint32_t lsite = (d & 1) ? nbq : st_site, lpar = (d & 1) ? 1u - p : p;
+          // with the tile's first hop, the next tile's link record
+          if (d == 0 && tile + (int)gridDim.x < ntiles) {
+            fetch_record(tile + (int)gridDim.x, it + 1);
+            fetched++;
+          }
+          const uint32_t nbq = sc.nb(A.geo, p, d);
           const uint32_t bar = ring_full + 8 * st, dst = smem0 + st * kStage;
           tma::mbar_expect_tx(bar, tx);
-          for (int h = 0; h < T.halves; h++)
-            tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0,
-                         (int)nbq, bar, keep);
-          // form 0 (rows of U) for forward hops, form 1 (rows of U^T) for backward ones
-          tcs::bulk_load(dst + kA,
-                         gtc + ((uint64_t)((d & 1) * 8 + 2 * (d >> 1) + lpar) * vh + lsite) * kLink, kLink, bar);
+          if (T.fused)
+            tcs::load_5d(dst, &map_in, 0, 0, 0, 2 * (int)st_chunk, (int)nbq, bar, keep);
+          else
+            for (int h = 0; h < T.halves; h++)
+              tcs::load_4d(dst + (uint32_t)h * tcs::kHalfBytes, &map_in, (int)(st_chunk * T.rt) + 32 * h, 0, 0,
+                           (int)nbq, bar, keep);
         }
       }
       // copies still in flight land before the CTA's shared memory is released (bounded):
@@ -398,6 +447,11 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
       for (uint32_t k = 0; k < (uint32_t)NST && k < qq; k++) {
         const uint32_t last = qq - 1 - k;
         tma::mbar_wait(ring_full + 8 * (last % NST), (last / NST) & 1u, T.err);
+      }
+      // and the last record issued into each slot
+      for (int k = 0; k < tcs::kRecSlots && k < fetched; k++) {
+        const int last = fetched - 1 - k;
+        tma::mbar_wait(rec_full + 8 * (last % tcs::kRecSlots), (last / tcs::kRecSlots) & 1u, T.err);
       }
     }
   } else {
@@ -409,21 +463,17 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
     const __nv_bfloat16* __restrict__ xin = static_cast<const __nv_bfloat16*>(A.x);
     __nv_bfloat16* __restrict__ out = static_cast<__nv_bfloat16*>(A.out);
     int it = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+    // warps whose 32 accumulator lanes are all padding rows (tiles of at most
+    // 32 RHS) have nothing to read and take no part in the hand-off
+    const int first = lq < tcs::epilogue_warps(T.rt) ? (int)blockIdx.x : ntiles;
+    for (int tile = first; tile < ntiles; tile += gridDim.x, it++) {
       const uint32_t site = (uint32_t)(tile / T.chunks), chunk = (uint32_t)(tile % T.chunks);
       const uint32_t rhs = chunk * (uint32_t)T.rt + r;
       const bool live = r < (uint32_t)T.rt && (!A.mask || A.mask[rhs] != 0);
       const float ca = live ? (A.a_rhs_f ? A.a_rhs_f[rhs] : A.af) : 0.f;
       const uint32_t acc = (uint32_t)it & 1u;
-      if (!tcs::wait(tmem_full + 8 * acc, ((uint32_t)it >> 1) & 1u, T.err, abort_flag)) break;
+      if (!tcs::wait_sleep(tmem_full + 8 * acc, ((uint32_t)it >> 1) & 1u, T.err, abort_flag)) break;
       tc::fence_after();
-      if (lq * 16u >= (uint32_t)T.rt) {
-        // this warp's 32 accumulator lanes are padding rows (tiles of at most
-        // 32 RHS): nothing to read, release the accumulator for its tile after next
-        tc::fence_before();
-        tma::mbar_arrive(tmem_empty + 8 * acc);
-        continue;
-      }
       const uint32_t lane_addr = tmem + ((lq * 32u) << 16) + acc * 64u;
       // Re (ri = 0) = Re K - partner's Im K, Im (ri = 1) = Re K + partner's Im K;
       // component k of this lane's output at o + k * step (BF16 halves)

@@ -143,6 +143,20 @@ bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool tma_encode_field_swizzled_halves(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major) {
+  if (nrhs % 32) return false;
+  // byte strides of colour, spin, half (32 RHS) and site
+  const cuuint64_t cs = site_major ? (cuuint64_t)nrhs * 4 : (cuuint64_t)vh * nrhs * 4;
+  const cuuint64_t ss = site_major ? (cuuint64_t)4 * N * nrhs * 4 : (cuuint64_t)nrhs * 4;
+  const cuuint64_t dims[5] = {32, (cuuint64_t)N, 4, (cuuint64_t)nrhs / 32, (cuuint64_t)vh};
+  const cuuint64_t strides[4] = {cs, (cuuint64_t)N * cs, 128, ss};
+  const cuuint32_t box[5] = {32, 8, 4, 2, 1};
+  const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+  return encode_fn()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<void*>(ptr), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rcta, int hx) {
   const cuuint64_t dims[3] = {(cuuint64_t)nrhs, (cuuint64_t)vh, 1};
   const cuuint64_t strides[2] = {(cuuint64_t)nrhs * 4, (cuuint64_t)vh * nrhs * 4};

@@ -35,6 +35,10 @@ void tma_encode_norm(CUtensorMap* m, const float* ptr, int nrhs, int vh, int rct
 // 8 colours, 4 spins, 1 site), 128-byte swizzle, colours N..7 zero-filled;
 // false when the driver rejects the map
 bool tma_encode_field_swizzled(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major);
+// the same field with the RHS index split as 32 x (nrhs / 32) (nrhs a multiple
+// of 32): dims (RHS 32, colour, spin, half, site), box (32, 8, 4, 2, 1), so
+// that one copy lands two 32-RHS halves 4 KB apart in shared memory
+bool tma_encode_field_swizzled_halves(CUtensorMap* m, const void* ptr, int nrhs, int vh, int N, bool site_major);
 
 // Tile plan for (precision, N, geometry, nrhs, R, stages); rcta = 0 picks the
 // largest RHS chunk that fits.  False when the staged kernel cannot run these

@@ -476,14 +476,22 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
 
 namespace {
 // one thread per 4-byte word (two BF16 of adjacent columns) of the destination
-__global__ void gauge_tc_rows_kernel(const double2* __restrict__ src, uint32_t* __restrict__ dst, int64_t vh,
-                                     int N) {
-  const int64_t n = 2 * 8 * vh * 64;  // 64 words per link and form
+__global__ void gauge_tc_records_kernel(const double2* __restrict__ src, uint32_t* __restrict__ dst, Geometry geo,
+                                        int N) {
+  const int64_t vh = geo.vh;
+  const int64_t n = 2 * vh * 8 * 64;  // 64 words per link
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const int w = (int)(i & 63);
-    const int64_t link = i >> 6;  // (form * 8 + blk) * vh + site
-    const int64_t site = link % vh, fb = link / vh, blk = fb % 8, form = fb / 8;
+    const int d = (int)((i >> 6) & 7);
+    const int64_t ps = i >> 9;  // p * vh + site
+    const uint32_t site = (uint32_t)(ps % vh), p = (uint32_t)(ps / vh);
+    // hop d = 2 mu + b: forward hops multiply by U_mu(x) (rows of U, form 0),
+    // backward hops by U_mu(x - mu)^dag (rows of U^T, form 1) from the other parity
+    const int mu = d >> 1, form = d & 1;
+    const uint32_t lpar = form ? 1u - p : p;
+    const uint32_t lsite = form ? EoSite(geo, site).nb(geo, p, d) : site;
+    const int64_t blk = 2 * mu + lpar;
     const int part = w >> 5, row = (w >> 2) & 7, c0 = 2 * (w & 3);
     float v[2] = {0.f, 0.f};
 #pragma unroll
@@ -491,7 +499,7 @@ __global__ void gauge_tc_rows_kernel(const double2* __restrict__ src, uint32_t* 
       const int col = c0 + k;
       if (row < N && col < N) {
         const int comp = form == 0 ? row * N + col : col * N + row;  // U[row][col] or U[col][row]
-        const double2 u = src[(blk * N * N + comp) * vh + site];
+        const double2 u = src[(blk * N * N + comp) * vh + lsite];
         v[k] = (float)(part ? u.y : u.x);
       }
     }
@@ -501,11 +509,11 @@ __global__ void gauge_tc_rows_kernel(const double2* __restrict__ src, uint32_t* 
 }
 }  // namespace
 
-void gauge_tc_rows_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st) {
+void gauge_tc_records_bf16(int N, const void* src_fp64, void* dst, const Geometry& geo, cudaStream_t st) {
   const int block = 256;
-  const int grid = (int)std::min<int64_t>((2 * 8 * vh * 64 + block - 1) / block, 152 * 32);
-  gauge_tc_rows_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), static_cast<uint32_t*>(dst), vh,
-                                               N);
+  const int grid = (int)std::min<int64_t>((2 * (int64_t)geo.vh * 8 * 64 + block - 1) / block, 152 * 32);
+  gauge_tc_records_kernel<<<grid, block, 0, st>>>(static_cast<const double2*>(src_fp64), static_cast<uint32_t*>(dst),
+                                                  geo, N);
   QCU_CHECK_CUDA(cudaGetLastError());
 }
 

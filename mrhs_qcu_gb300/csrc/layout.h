@@ -43,16 +43,19 @@ void compress_gauge_su3(const void* src_fp64, int prec, void* dst, int64_t vh, c
 // max over the links of |row 2 - conj(row 0 x row 1)| (0 for exact SU(3));
 // scratch: one device unsigned
 double su3_row_deviation(const void* src_fp64, int64_t vh, unsigned* scratch, cudaStream_t st);
-// BF16 links for the spinor-operand tensor-core dslash, site-major and
-// already split into the rows its link operand is built from:
-// [form 2][8 (mu, parity)][Vh][part 2][row 8][col 8] BF16, 256 bytes per link
-// and form (one bulk copy), rows and columns >= N zero.  Form 0 holds the
-// rows of U (part 0 Re, part 1 Im), for forward hops; form 1 the rows of U^T
-// (the columns of U), for backward hops, which use conj(U^T).  Built from the
-// FP64 master [8][N*N][Vh].
+// BF16 links for the spinor-operand tensor-core dslash, one record per output
+// site and parity holding the eight links its hops multiply by, already split
+// into the rows its link operand is built from:
+// [parity 2][Vh][hop 8][part 2][row 8][col 8] BF16, 256 bytes per link and
+// 2 KB per site (one bulk copy per site), rows and columns >= N zero.  Hop
+// d = 2 mu (forward) holds the rows of U_mu(x) (part 0 Re, part 1 Im); hop
+// 2 mu + 1 (backward) the rows of U_mu(x - mu)^T (the columns of that link),
+// which the hop uses conjugated.  Each link appears twice, as in a copy per
+// form.  Built from the FP64 master [8][N*N][Vh].
 constexpr int kTcLinkBytes = 256;
-inline size_t tc_links_bytes(int64_t vh) { return (size_t)2 * 8 * vh * kTcLinkBytes; }
-void gauge_tc_rows_bf16(int N, const void* src_fp64, void* dst, int64_t vh, cudaStream_t st);
+constexpr int kTcRecordBytes = 8 * kTcLinkBytes;
+inline size_t tc_links_bytes(int64_t vh) { return (size_t)2 * vh * kTcRecordBytes; }
+void gauge_tc_records_bf16(int N, const void* src_fp64, void* dst, const Geometry& geo, cudaStream_t st);
 // per-RHS coalesced arrays (the reference's internal layout, one [ncomp][vh]
 // complex array per RHS, include/basic_data/qcu_point.cuh:80-88 of the
 // reference) <-> one MRHS field [ncomp][vh][nrhs], FP32 or FP64 (no

@@ -155,6 +155,36 @@ inline Geometry make_geometry(const int L[4]) {
   return g;
 }
 
+// Coordinates of even-odd site s (its index within one parity, x halved) and
+// of its eight neighbours.  Hop d = 2 mu + (backward ? 1 : 0); p is the parity
+// of the site's half-field.  An x neighbour of a site whose (y + z + t) parity
+// eo differs from p sits at the same index or the next one (forward), at the
+// previous one or the same (backward).
+struct EoSite {
+  uint32_t site, xh, y, z, t, eo;
+  __host__ __device__ __forceinline__ EoSite(const Geometry& g, uint32_t s) : site(s) {
+    uint32_t rest, rest2;
+    g.div_hx.divmod(s, rest, xh);
+    g.div_y.divmod(rest, rest2, y);
+    g.div_z.divmod(rest2, t, z);
+    eo = (y + z + t) & 1u;
+  }
+  __host__ __device__ __forceinline__ uint32_t nb(const Geometry& g, uint32_t p, int d) const {
+    const uint32_t hx = (uint32_t)g.hx, ly = (uint32_t)g.L[1], lz = (uint32_t)g.L[2], lt = (uint32_t)g.L[3];
+    const uint32_t plane = (uint32_t)g.plane, cube = (uint32_t)g.cube;
+    switch (d) {
+      case 0: return (eo != p) ? (xh == hx - 1 ? site - (hx - 1) : site + 1) : site;
+      case 1: return (eo == p) ? (xh == 0 ? site + (hx - 1) : site - 1) : site;
+      case 2: return (y == ly - 1) ? site - (ly - 1) * hx : site + hx;
+      case 3: return (y == 0) ? site + (ly - 1) * hx : site - hx;
+      case 4: return (z == lz - 1) ? site - (lz - 1) * plane : site + plane;
+      case 5: return (z == 0) ? site + (lz - 1) * plane : site - plane;
+      case 6: return (t == lt - 1) ? site - (lt - 1) * cube : site + cube;
+      default: return (t == 0) ? site + (lt - 1) * cube : site - cube;
+    }
+  }
+};
+
 // ---------------------------------------------------------------------------
 // storage traits: how a complex number of precision P sits in memory and how
 // it converts to the compute type (double for FP64, float otherwise)

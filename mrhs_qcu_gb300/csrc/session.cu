@@ -353,7 +353,7 @@ const void* Session::gauge_tc() {
   QCU_REQUIRE(gauge_loaded_, QCU_ERR_NO_GAUGE, "localGauge_ is nullptr, not loaded.\n");
   if (!gauge_tc_valid_) {
     void* d = gauge_tc_.ensure(tc_links_bytes(geo.vh));
-    gauge_tc_rows_bf16(N, gauge_[PREC_DOUBLE].get(), d, geo.vh, stream());
+    gauge_tc_records_bf16(N, gauge_[PREC_DOUBLE].get(), d, geo, stream());
     gauge_tc_valid_ = true;
   }
   return gauge_tc_.get();
