@@ -610,14 +610,16 @@ def colors_bench(torch, Q, peak, fma):
     for n in (4, 6, 8):
         g_dev, psi = make_inputs(torch, L, n, 64, seed_g=300 + n, seed_p=301)
         # FP32: the autotuned CUDA-core kernel; BF16: CUDA cores (register kernel, R = 2) and the
-        # tensor-core (tcgen05) kernel, each pinned
+        # tensor-core (tcgen05) kernels, each pinned (spinor-operand variants 4 and 6: rings of 4 and
+        # 5 stages), and the autotuner's choice on site-major fields
         for p, pname, kernel, pin in ((1, "fp32", "cuda_core", None), (4, "bf16", "cuda_core", "2,64,1,0"),
                                       (4, "bf16", "tensor_core_projected", "1,0,0,0,0,0,1"),
                                       (4, "bf16", "tensor_core_projected_tma", "1,0,0,0,0,0,2"),
                                       (4, "bf16", "tensor_core_spinor", "1,0,0,0,0,0,4"),
-                                      (4, "bf16", "tensor_core_spinor_deep", "1,0,0,0,0,0,5"),
+                                      (4, "bf16", "tensor_core_spinor_ring5", "1,0,0,0,0,0,6"),
                                       (5, "bf16-site", "tensor_core_spinor", "1,0,0,0,0,0,4"),
-                                      (5, "bf16-site", "tensor_core_spinor_deep", "1,0,0,0,0,0,5")):
+                                      (5, "bf16-site", "tensor_core_spinor_ring5", "1,0,0,0,0,0,6"),
+                                      (5, "bf16-site", "tensor_core_tuned", None)):
             for nr in (16, 32, 64):
                 if pin:
                     os.environ["QCU_DSLASH_CONFIG"] = pin

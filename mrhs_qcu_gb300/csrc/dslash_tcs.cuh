@@ -30,15 +30,19 @@
 // each other through mbarriers only:
 //   warps 0-3  B builders: per hop, the 4 KB B operand into a ring of NB
 //              buffers, each thread two 16-byte chunks: signed copies of one
-//              link row of the tile's link record
+//              link row of the tile's link record.  They never read the A
+//              stage, so a hop's build overlaps the copy of its neighbour
+//              block instead of following it; only the MMA waits for both
+//              (waiting for the copy as well put the copy latency and the
+//              build in series: about 15% slower at nrhs 64)
 //   warp 4     MMA issuer (one thread): two MMAs per hop into one of two
 //              tensor-memory accumulators; commits free the B buffer and the
 //              TMA stage, and hand a finished tile to the epilogue
 //   warp 5     TMA producer (one thread): per hop, the neighbour's A block
 //              (one box, or two of 32 RHS) into a ring of NST stages, as far
-//              ahead as the ring allows; per tile, with its first hop, the
-//              site's link record (one 2 KB bulk copy, layout.h
-//              gauge_tc_records_bf16) into one of two record slots
+//              ahead as the ring allows; with each tile's first hop, the next
+//              tile's link record (one 2 KB bulk copy, layout.h
+//              gauge_tc_records_bf16) into one of three record slots
 //   warps 6-9  epilogue: tensor memory -> Re/Im combination -> global, one
 //              tile behind the MMAs (double-buffered accumulator)
 // Every wait is bounded (about 1 s); a timeout sets *err and a shared abort
@@ -121,19 +125,30 @@ __device__ __forceinline__ void ld8(uint32_t taddr, uint32_t (&r)[8]) {
                : "memory");
 }
 
-// 1-D bulk copy global -> shared (16-byte aligned, size a multiple of 16), completion counted on bar
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
 // L2 policy that keeps lines resident (each neighbour block is read by the
 // eight sites around it, a short while apart)
 __device__ __forceinline__ uint64_t evict_last_policy() {
   uint64_t pol;
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
   return pol;
+}
+// L2 policy for data read once (the link records): evicted first, so that it
+// does not displace the neighbour blocks that are read again
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+
+// 1-D bulk copy global -> shared with an L2 cache policy (16-byte aligned,
+// size a multiple of 16), completion counted on bar
+__device__ __forceinline__ void bulk_load_hint(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar,
+                                               uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar), "l"(policy)
+      : "memory");
 }
 
 // 5-D tiled TMA load into shared memory with an L2 cache policy, completion counted on bar
@@ -217,14 +232,12 @@ __device__ __forceinline__ bool wait_sleep(uint32_t bar, uint32_t parity, int* e
 // BF16 (strides of either layout), box (32 RHS, 8 colours, 4 spins, 1 site),
 // 128-byte swizzle; or, when the RHS count is a multiple of 32 and a tile
 // holds 64 RHS (T.fused), as [site][half][spin][colour][RHS 32] with box
-// (32, 8, 4, 2, 1), which lands a tile's two halves in one copy.  The copy
-// engine's cost per copy hardly depends on its size, and with 4 CTAs per SM
-// the producer spends most of each hop waiting to issue, so the copies per
-// site are what count.  In the site-major layout a box is one contiguous run
-// of the field; in the component-major one it gathers rows of 128 bytes from
-// arrays Vh x nrhs x 4 bytes apart, which the copy engine serves at about
-// half the rate.  The links come from A.gauge_tc: one 2 KB record per site
-// (its eight links in row form), one bulk copy per tile.
+// (32, 8, 4, 2, 1), which lands a tile's two halves in one copy.  In the
+// site-major layout a box is one contiguous run of the field; in the
+// component-major one it gathers rows of 128 bytes from arrays Vh x nrhs x 4
+// bytes apart, which the copy engine serves at about half the rate.  The
+// links come from A.gauge_tc: one 2 KB record per site (its eight links in
+// row form), one bulk copy per tile, a tile ahead.
 template <int N, int NST, int NB, int HV>
 __global__ void __launch_bounds__(tcs::kThreads, 4)
     wilson_tcs_kernel(const __grid_constant__ TcsDslashArgs T, const __grid_constant__ CUtensorMap map_in) {
@@ -399,7 +412,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
       const unsigned char* gtc = static_cast<const unsigned char*>(A.gauge_tc);
       const uint32_t vh = A.geo.vh;
       const uint32_t tx = (uint32_t)T.halves * tcs::kHalfBytes;
-      const uint64_t keep = tcs::evict_last_policy();
+      const uint64_t keep = tcs::evict_last_policy(), once = tcs::evict_first_policy();
       uint32_t qq = 0;
       bool ok = true;
       int it = 0;
@@ -407,8 +420,9 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
       auto fetch_record = [&](int tile_r, int it_r) {
         const uint32_t bar = rec_full + 8 * (it_r % tcs::kRecSlots);
         tma::mbar_expect_tx(bar, tcs::kRecBytes);
-        tcs::bulk_load(smem0 + tcs::rec_off(NST, HV) + (uint32_t)(it_r % tcs::kRecSlots) * tcs::kRecBytes,
-                       gtc + ((uint64_t)p * vh + (uint32_t)(tile_r / T.chunks)) * tcs::kRecBytes, tcs::kRecBytes, bar);
+        tcs::bulk_load_hint(smem0 + tcs::rec_off(NST, HV) + (uint32_t)(it_r % tcs::kRecSlots) * tcs::kRecBytes,
+                            gtc + ((uint64_t)p * vh + (uint32_t)(tile_r / T.chunks)) * tcs::kRecBytes, tcs::kRecBytes,
+                            bar, once);
       };
       int fetched = 0;  // records issued
       if ((int)blockIdx.x < ntiles) {

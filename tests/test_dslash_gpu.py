@@ -207,7 +207,7 @@ def test_tensor_core_kernel(cuda, qcu_lib, n, nrhs, variant):
     antiperiodic t, RHS counts that fill the 128 MMA rows, leave them partly
     empty, take two tiles, or end inside the second 32-RHS box.  Variants 1-3
     are the projected half-spinor kernel (N >= 4; the TMA ring for N = 4, 6,
-    8), 4-6 the spinor-operand kernel with 2-4 ring stages, 7-8 the same with
+    8), 4-6 the spinor-operand kernel with 4-6 ring stages, 7-8 the same with
     deeper rings of one 32-RHS half per stage (launched for tiles of at most
     32 RHS; larger tiles run another kernel)."""
     L = (4, 4, 4, 8)

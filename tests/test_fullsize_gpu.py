@@ -114,8 +114,10 @@ def test_solve_benchmark_workload(cuda, qcu_lib, inner):
 # (kernel name, storage precision, QCU_DSLASH_CONFIG pin or None for the autotuner)
 SUN_KERNELS = [("cuda_core_fp32", 1, None), ("cuda_core_bf16", 4, "2,64,1,0"),
                ("tensor_core_projected", 4, "1,0,0,0,0,0,1"), ("tensor_core_projected_tma", 4, "1,0,0,0,0,0,2"),
-               ("tensor_core_spinor", 4, "1,0,0,0,0,0,4"), ("tensor_core_spinor_deep", 4, "1,0,0,0,0,0,5"),
-               ("tensor_core_spinor_site_major", 5, "1,0,0,0,0,0,4")]
+               ("tensor_core_spinor", 4, "1,0,0,0,0,0,4"), ("tensor_core_spinor_ring5", 4, "1,0,0,0,0,0,6"),
+               ("tensor_core_spinor_site_major", 5, "1,0,0,0,0,0,4"),
+               ("tensor_core_spinor_site_major_ring5", 5, "1,0,0,0,0,0,6"),
+               ("tensor_core_site_major_tuned", 5, None)]
 
 
 @pytest.mark.parametrize("nrhs", [16, 32, 64])
