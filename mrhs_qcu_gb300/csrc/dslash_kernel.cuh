@@ -29,7 +29,7 @@ namespace qcu {
 struct DslashArgs {
   const void* gauge;     // [4][2][N*N][Vh] complex<P>
   const void* gauge12 = nullptr;  // SU(3): [4][2][6][Vh], the first two rows (or nullptr)
-  const void* gauge_tc = nullptr; // BF16 link rows (layout.h gauge_tc_rows_bf16) for the tensor-core dslash, or nullptr
+  const void* gauge_tc = nullptr; // BF16 per-site link records (layout.h gauge_tc_records_bf16) for the tensor-core dslash, or nullptr
   const void* in;        // MRHS field, parity 1 - parity
   const float* in_norm;  // [Vh][nrhs] (16-bit storage only)
   void* out;             // MRHS field, output parity

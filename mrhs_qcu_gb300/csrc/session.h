@@ -161,9 +161,9 @@ class Session {
   // `prec`), or nullptr when the loaded field is not SU(3) to that precision's
   // rounding (then the third rows are not reconstructible)
   const void* gauge12(int prec);
-  // the links in BF16, site-major and split into rows (layout.h
-  // gauge_tc_rows_bf16), for the spinor-operand tensor-core dslash; built on
-  // first use
+  // the links in BF16 as per-site records split into rows (layout.h
+  // gauge_tc_records_bf16), for the spinor-operand tensor-core dslash; built
+  // on first use
   const void* gauge_tc();
 
   // ---- clover term (clover.h) ---------------------------------------------
