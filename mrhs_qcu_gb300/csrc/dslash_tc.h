@@ -34,6 +34,15 @@ constexpr int tcs_stages(int variant) { return variant == 5 ? 6 : variant == 6 ?
 constexpr int tcs_bbufs(int variant) { return variant == 6 ? 2 : variant == 8 ? 4 : 3; }
 constexpr int tcs_halves(int variant) { return variant >= 7 ? 1 : 2; }
 
+// Variants 4 and 6-8 are sized so that 4 CTAs share an SM (228 KB of shared
+// memory, 1 KB reserved per CTA; tensor memory 4 x 128 columns); variant 5
+// trades the fourth CTA for six stages.
+constexpr bool tcs_fits_4_ctas(int v) {
+  return 4 * (tcs::smem_bytes(tcs_stages(v), tcs_bbufs(v), tcs_halves(v)) + 1024) <= 228 * 1024;
+}
+static_assert(tcs_fits_4_ctas(4) && tcs_fits_4_ctas(6) && tcs_fits_4_ctas(7) && tcs_fits_4_ctas(8),
+              "a spinor-operand variant no longer fits 4 CTAs per SM");
+
 template <int N, int V>
 void launch_wilson_tcs(const DslashArgs& A, cudaStream_t st) {
   constexpr int NST = tcs_stages(V), NB = tcs_bbufs(V), HV = tcs_halves(V);
