@@ -31,7 +31,7 @@ bool tcs_plan(const DslashArgs& A, int N, TcsDslashArgs* T, CUtensorMap* map_in)
 // their deeper rings fit the same shared memory; they take tiles of at most
 // 32 RHS (nrhs <= 32, or RHS counts that split into such tiles).
 constexpr int tcs_stages(int variant) { return variant == 5 ? 6 : variant == 6 ? 5 : variant == 7 ? 8 : variant == 8 ? 6 : 4; }
-constexpr int tcs_bbufs(int variant) { return variant == 6 ? 2 : variant == 8 ? 4 : 3; }
+constexpr int tcs_bbufs(int variant) { return (variant == 6 || variant == 7 || variant == 8) ? 2 : 3; }
 constexpr int tcs_halves(int variant) { return variant >= 7 ? 1 : 2; }
 
 // Variants 4 and 6-8 are sized so that 4 CTAs share an SM (228 KB of shared
@@ -91,7 +91,7 @@ void launch_wilson_tc(const DslashArgs& A, cudaStream_t st) {
 // variant: 1 = direct loads, 2 / 3 = TMA ring of 2 / 3 stages (projected
 // half-spinor operands, dslash_tc.cuh); 4 / 5 / 6 = the spinor-operand kernel
 // (dslash_tcs.cuh) with (TMA stages, B buffers) = (4, 3) / (6, 3) / (5, 2);
-// 7 / 8 = the same with one 32-RHS half per stage, (8, 3) / (6, 4)
+// 7 / 8 = the same with one 32-RHS half per stage, (8, 2) / (6, 2)
 constexpr int kTcVariants = 8;  // <= 15 (registry keys)
 using TcLauncher = void (*)(const DslashArgs&, cudaStream_t);
 void register_tc(int prec, int N, int variant, TcLauncher fn);
