@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(tcs::kThreads, 4)
             break;
           }
           // with the tile's first hop, the next tile's link record
-          if (d == 0 && tile + (int)gridDim.x < ntiles) {
+          if (d == 0 && tile < ntiles - (int)gridDim.x) {
             fetch_record(tile + (int)gridDim.x, it + 1);
             fetched++;
           }
