@@ -106,7 +106,8 @@ def test_tensor_core_operands_reproduce_the_hop(n, parity, dagger, ap):
 # B[k][n]: n = 32 part + 8 s + a (part 0 / 1 = Re / Im of K_hop), the real
 # split of K_hop^T, K_hop[(s, a)][(s', b)] = bc P[s][s'] W[a][b], built in
 # 16-byte chunks (fixed n, 8 consecutive k = one input spin) as signed copies
-# of the rows Re W[a][.] / Im W[a][.].  D = sum over hops of A B; the
+# of the rows Re W[a][.] / Im W[a][.], read from the site's link record
+# (link_records).  D = sum over hops of A B; the
 # epilogue forms Re out = D[(r,Re)][ReK] - D[(r,Im)][ImK] and
 # Im out = D[(r,Im)][ReK] + D[(r,Re)][ImK].
 
@@ -122,40 +123,71 @@ def chunk_code(mu, fwd, s, g, dagger, bc):
     return mu in (0, 2), sg  # z = sg * (i if imaginary gamma row)
 
 
+def eo_neighbour(site, d, p, L):
+    """Index of the neighbour of even-odd site `site` (parity p) for hop
+    d = 2 mu + (backward), in the other parity's half-field."""
+    hx, Ly, Lz, Lt = L[0] // 2, L[1], L[2], L[3]
+    plane, cube = hx * Ly, hx * Ly * Lz
+    xh, rest = site % hx, site // hx
+    y, rest2 = rest % Ly, rest // Ly
+    z, t = rest2 % Lz, rest2 // Lz
+    eo = (y + z + t) & 1
+    mu, fwd = d >> 1, (d & 1) == 0
+    if mu == 0:
+        if fwd:
+            return (site - (hx - 1) if xh == hx - 1 else site + 1) if eo != p else site
+        return (site + (hx - 1) if xh == 0 else site - 1) if eo == p else site
+    if mu == 1:
+        return (site - (Ly - 1) * hx if y == Ly - 1 else site + hx) if fwd else \
+               (site + (Ly - 1) * hx if y == 0 else site - hx)
+    if mu == 2:
+        return (site - (Lz - 1) * plane if z == Lz - 1 else site + plane) if fwd else \
+               (site + (Lz - 1) * plane if z == 0 else site - plane)
+    return (site - (Lt - 1) * cube if t == Lt - 1 else site + cube) if fwd else \
+           (site + (Lt - 1) * cube if t == 0 else site - cube)
+
+
+def link_records(g, L):
+    """The spinor-operand kernel's per-site link records (layout.h
+    gauge_tc_records_bf16), in FP64: [parity][Vh][hop 8][part 2][row 8][col 8].
+    Hop 2 mu holds the rows of U_mu(x) (the site's own parity), hop 2 mu + 1
+    the rows of U_mu(x - mu)^T, the link of the backward neighbour (other
+    parity); part 0 / 1 = Re / Im, rows and columns >= N zero."""
+    N = g.shape[-1]
+    vh = g.shape[2]
+    rec = np.zeros((2, vh, 8, 2, 8, 8))
+    for p in range(2):
+        for site in range(vh):
+            for d in range(8):
+                mu = d >> 1
+                if d & 1:
+                    u = g[mu, 1 - p, eo_neighbour(site, d, p, L)].T
+                else:
+                    u = g[mu, p, site]
+                rec[p, site, d, 0, :N, :N] = u.real
+                rec[p, site, d, 1, :N, :N] = u.imag
+    return rec
+
+
 def tcs_hop(psi, g, L, p, dagger, antiperiodic):
     nrhs, vh, _, N = psi.shape
     hx, Ly, Lz, Lt = L[0] // 2, L[1], L[2], L[3]
-    plane, cube = hx * Ly, hx * Ly * Lz
+    cube = hx * Ly * Lz
+    records = link_records(g, L)
     out = np.zeros_like(psi)
     for site in range(vh):
-        xh, rest = site % hx, site // hx
-        y, rest2 = rest % Ly, rest // Ly
-        z, t = rest2 % Lz, rest2 // Lz
-        eo = (y + z + t) & 1
+        t = site // cube
         d = np.zeros((2 * nrhs, 64))
         for hop in range(8):
             mu, fwd, bc = hop >> 1, (hop & 1) == 0, 1.0
-            if mu == 0:
-                if fwd:
-                    nb = (site - (hx - 1) if xh == hx - 1 else site + 1) if eo != p else site
-                else:
-                    nb = (site + (hx - 1) if xh == 0 else site - 1) if eo == p else site
-            elif mu == 1:
-                nb = (site - (Ly - 1) * hx if y == Ly - 1 else site + hx) if fwd else \
-                     (site + (Ly - 1) * hx if y == 0 else site - hx)
-            elif mu == 2:
-                nb = (site - (Lz - 1) * plane if z == Lz - 1 else site + plane) if fwd else \
-                     (site + (Lz - 1) * plane if z == 0 else site - plane)
-            else:
-                nb = (site - (Lt - 1) * cube if t == Lt - 1 else site + cube) if fwd else \
-                     (site + (Lt - 1) * cube if t == 0 else site - cube)
-                if antiperiodic and (t == Lt - 1 if fwd else t == 0):
-                    bc = -1.0
-            u = g[mu, p, site] if fwd else g[mu, 1 - p, nb]
-            w = u if fwd else np.conj(u.T)
-            # rows Re W[a][.], Im W[a][.], padded to 8 x 8
-            wrow = np.zeros((2, 8, 8))
-            wrow[0, :N, :N], wrow[1, :N, :N] = w.real, w.imag
+            nb = eo_neighbour(site, hop, p, L)
+            if mu == 3 and antiperiodic and (t == Lt - 1 if fwd else t == 0):
+                bc = -1.0
+            # rows Re W[a][.], Im W[a][.] from the site's record: W = U (forward), or
+            # conj(U^T) (backward), whose Im rows the builders negate
+            wrow = records[p, site, hop].copy()
+            if not fwd:
+                wrow[1] = -wrow[1]
             a_op = np.zeros((2 * nrhs, 32))
             for r in range(nrhs):
                 for sp in range(4):
@@ -190,3 +222,23 @@ def test_spinor_operand_formulation_reproduces_the_hop(n, parity, dagger, ap):
     got = tcs_hop(psi, g, L, parity, dagger, ap)
     ref = O.dslash(psi, g, L, parity, dagger, ap)
     assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-13
+
+
+@pytest.mark.parametrize("L", [(4, 2, 2, 4), (6, 4, 2, 2), (2, 2, 2, 2)])
+def test_link_records_hold_every_link_twice(L):
+    """The per-site records hold each link twice: as rows of U in its own
+    site's forward hop, and transposed in exactly one backward hop of the
+    other parity (the site it is the backward neighbour of)."""
+    n = 3
+    g = S.random_gauge(L, n, seed=21)
+    rec = link_records(g, L)
+    vh = g.shape[2]
+    for p in range(2):
+        for mu in range(4):
+            fwd = rec[p, :, 2 * mu, 0, :n, :n] + 1j * rec[p, :, 2 * mu, 1, :n, :n]
+            assert np.array_equal(fwd, g[mu, p])
+            bwd = rec[p, :, 2 * mu + 1, 0, :n, :n] + 1j * rec[p, :, 2 * mu + 1, 1, :n, :n]
+            nbs = [eo_neighbour(s, 2 * mu + 1, p, L) for s in range(vh)]
+            assert sorted(nbs) == list(range(vh))  # a permutation of the other parity's sites
+            for s in range(vh):
+                assert np.array_equal(bwd[s], g[mu, 1 - p, nbs[s]].T)
