@@ -332,43 +332,46 @@ def run_gpu(args):
     if not args.skip_e2e:
         # Pinned host buffers in and out; every step uploads its 12 sources,
         # runs the drop-in ABI (pushBackFermions x 12, startDslash) and
-        # downloads its 12 results.  Device buffers are double buffered and the
+        # downloads its 12 results.  Device buffers are triple buffered and the
         # copies run on their own streams, so step k+1's upload and step k-1's
         # download overlap step k (the two directions of the host link run
-        # concurrently).
+        # concurrently), and the next upload does not wait for step k's
+        # compute: with two buffers both directions of the link stood idle
+        # while a step computed.
         host_in = [torch.empty((vh, 4, n), dtype=torch.complex128).pin_memory() for _ in range(nrhs)]
         for r in range(nrhs):
             host_in[r].copy_(psi_dev[r])
         host_out = [torch.empty((vh, 4, n), dtype=torch.complex128).pin_memory() for _ in range(nrhs)]
+        nbuf = 3
         dev_in = [[torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
-                  for _ in range(2)]
+                  for _ in range(nbuf)]
         dev_out = [[torch.empty((vh, 4, n), dtype=torch.complex128, device="cuda") for _ in range(nrhs)]
-                   for _ in range(2)]
+                   for _ in range(nbuf)]
         s_up, s_down, s_comp = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
-        up_done = [torch.cuda.Event() for _ in range(2)]
-        comp_done = [torch.cuda.Event() for _ in range(2)]
-        down_done = [torch.cuda.Event() for _ in range(2)]
+        up_done = [torch.cuda.Event() for _ in range(nbuf)]
+        comp_done = [torch.cuda.Event() for _ in range(nbuf)]
+        down_done = [torch.cuda.Event() for _ in range(nbuf)]
         Q.set_stream(s_comp.cuda_stream)
 
         def upload(k):
-            b = k % 2
-            s_up.wait_event(comp_done[b])  # step k - 2 has read dev_in[b]
+            b = k % nbuf
+            s_up.wait_event(comp_done[b])  # step k - nbuf has read dev_in[b]
             with torch.cuda.stream(s_up):
                 for r in range(nrhs):
                     dev_in[b][r].copy_(host_in[r], non_blocking=True)
             up_done[b].record(s_up)
 
         def compute(k):
-            b = k % 2
+            b = k % nbuf
             s_comp.wait_event(up_done[b])
-            s_comp.wait_event(down_done[b])  # step k - 2's results have left dev_out[b]
+            s_comp.wait_event(down_done[b])  # step k - nbuf's results have left dev_out[b]
             for r in range(nrhs):
                 Q.pushBackFermions(dev_out[b][r].data_ptr(), dev_in[b][r].data_ptr())
             Q.startDslash(0, 0)
             comp_done[b].record(s_comp)
 
         def download(k):
-            b = k % 2
+            b = k % nbuf
             s_down.wait_event(comp_done[b])
             with torch.cuda.stream(s_down):
                 for r in range(nrhs):
@@ -414,7 +417,7 @@ def run_gpu(args):
                "host_link": link, "link_bound_ms_per_step": round(link_ms, 3),
                "frac_of_link_bound": round(link_ms / ems, 4),
                "path": "pinned host -> upload stream -> pushBackFermions x12 + startDslash -> download stream -> "
-                       "pinned host (FP64 caller layout); device buffers double buffered so step k+1's upload "
+                       "pinned host (FP64 caller layout); device buffers triple buffered so step k+1's upload "
                        "and step k-1's download overlap step k",
                "results_equal_device_path": e2e_same}
         Q.set_stream(None)
